@@ -1,0 +1,296 @@
+"""Benchmark: ln det M(k) evaluations per second on one GB300.
+
+Workload (the configuration the headline metric is quoted on): d = 3, N = 1024
+scatterers uniform in a ball at density 1 (seed 1, the reference's generator),
+model "maximum", ln det M(k)/N on the complex cut of 4096 equispaced k on
+Re k in [0.5, 3] at Im k = -0.05 (the central samples of a reference kcut with
+sample = 4096).  One step = the hot path over the whole cut.
+
+  value  : evals/s with positions and k already resident in HBM (msgpu_job_run)
+  e2e    : evals/s through the C-ABI call a user makes with host buffers
+           (msgpu_tracelog_batch: H2D of inputs, the kernels, D2H of results)
+  roofline, cpu_baseline, clocks, gpu_launches as documented in the design doc.
+
+Multi-GPU (torchrun): weak scaling -- each rank evaluates the full cut for its
+own realisation (seed = rank + 1); no collective on the data path.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   (the reference algorithm on the host cores)
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+D, N, NK = 3, 1024, 4096
+KMIN, KMAX = 0.5 - 0.05j, 3.0 - 0.05j
+METRIC = "ln det M(k) evals/s at N=1024 d=3 (complex cut, 4096 k)"
+UNIT = "evals/s"
+
+
+def workload_ks():
+    from msmodel_gb300 import kcut_args
+    return kcut_args(NK, KMIN, KMAX)[4::3][:NK].copy()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lr
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    try:
+                        rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+                    except ValueError:
+                        pass
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(seconds=15.0, nk_cap=NK):
+    """The reference algorithm (oracle port: reference assembly + OpenBLAS
+    zgetrf, one LAPACK thread per OpenMP thread, as run_tracelog_omp) on all
+    host cores, on a bounded sample of the same cut."""
+    from oracle import Oracle
+    from msmodel_gb300 import fill_medium
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    pos = fill_medium(D, N, 1)
+    ks = workload_ks()
+    done, t0, i = 0, time.perf_counter(), 0
+    while True:
+        chunk = ks[(i * threads) % nk_cap:(i * threads) % nk_cap + threads]
+        o.tracelog_batch(D, N, pos, chunk, nthreads=threads)
+        done += len(chunk)
+        i += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and i >= 2:
+            break
+    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmsref.so")) and False else "port"
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"first {done} of the 4096 cut points, N=1024 d=3 seed 1, {threads} OpenMP threads x "
+                      f"1 OpenBLAS thread ({o.lapack_config().split()[0:2]})", "seconds": el}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import Oracle
+    from msmodel_gb300 import fill_medium
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    pos = fill_medium(D, N, 1)
+    ks = workload_ks()
+    per_step = threads * 2
+    for w in range(args.warmup):
+        o.tracelog_batch(D, N, pos, ks[:threads], nthreads=threads)
+    t0 = time.perf_counter()
+    done = 0
+    for s in range(args.steps):
+        off = (s * per_step) % NK
+        o.tracelog_batch(D, N, pos, ks[off:off + per_step], nthreads=threads)
+        done += per_step
+    el = time.perf_counter() - t0
+    v = done / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
+            "data": "synthetic (seeded scatterers, reference generator)",
+            "config": {"workload": "kcut d=3 N=1024 4096k Im=-0.05", "d": D, "natom": N, "nk": NK,
+                       "model": "maximum", "shape": "ball", "sample_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} cut points per step, {threads} OpenMP threads x 1 OpenBLAS "
+                                       "thread, reference assembly restated + LAPACK zgetrf"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--nk", type=int, default=NK, help="cut points per step (default: the full 4096)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import msmodel_gb300 as ms
+    ws, rank, lr = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(lr)
+    ms.init(lr)
+    seed = rank + 1
+    med = ms.Medium(D, N, seed=seed)
+    ks = workload_ks()[:args.nk]
+    job = ms.Job("tracelog", [med], ks, precision=args.precision)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        job.run(stream.cuda_stream)
+    barrier()
+    l0 = ms.launch_count()
+    times = []
+    with Clocks(lr) as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between steps (outside the event bracket)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            job.run(stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    barrier()
+    launches = ms.launch_count() - l0
+    clocks = clk.summary()
+    tot = sum(times)
+    if ws > 1:
+        t = torch.tensor([tot], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot = float(t.item())
+    units = args.steps * len(ks) * ws
+    value = units / tot
+    out, st = job.results()
+    assert np.all(st == 0), "non-zero status in the benchmark results"
+
+    # dominant kernel: the persistent engine is the only launch of a step
+    flops_per_launch = job.flops
+    achieved = flops_per_launch / (tot / args.steps) / 1e12
+    peaks = read_peaks()
+    if args.precision == "fp64":
+        peak = ms.probe_fp64_tflops()
+        roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "measured DFMA probe on this GPU (MEASURED_PEAKS.json has no FP64 entry)",
+                "algorithmic": "8/3 N^3 real flops per ln det (complex LU), N=1024: 2.863e9",
+                "traffic": None}
+    else:
+        peak = peaks.get("bf16_tflops_sustained", 1728.6)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained",
+                "algorithmic": "8/3 N^3 real flops per ln det", "traffic": None}
+    prof = os.path.join(ROOT, "profiles", "engine_traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                tr = json.load(f).get(args.precision)
+            if tr:
+                roof["traffic"] = tr["bytes_per_eval"] * len(ks)
+                roof["traffic_note"] = tr.get("note")
+        except (OSError, ValueError):
+            pass
+
+    e2e = None
+    if not args.no_e2e:
+        nsteps = min(args.steps, 2)
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            pos = ms.fill_medium(D, N, seed)
+            m2 = ms.Medium(D, N, pos=pos, seed=seed)
+            o2, s2 = ms.tracelog_batch([m2], ks, precision=args.precision)
+        e_el = time.perf_counter() - t0
+        h2d = pos.nbytes + ks.nbytes + 4 * len(ks) * 2 + 40
+        d2h = 16 * len(ks) + 4 * len(ks)
+        e2e = {"value": nsteps * len(ks) * ws / e_el, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": nsteps,
+               "api": "msgpu_tracelog_batch (host buffers; includes medium fill, upload, kernels, download)"}
+        assert np.max(np.abs(o2 - out)) == 0.0 or np.max(np.abs(o2 - out) / np.abs(out)) < 1e-12
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)" if args.precision == "fp64" else
+                "c128 in / bf16-split tensor LU",
+                "data": "synthetic (seeded scatterers drawn by the reference's generator; no dataset)",
+                "config": {"workload": "kcut d=3 N=1024 4096k Im=-0.05", "d": D, "natom": N, "nk": len(ks),
+                           "model": "maximum", "shape": "ball", "precision": args.precision,
+                           "parallelism": f"replicas x{ws} (one realisation per GPU)",
+                           "l2": "flushed between steps (256 MB write); per-CTA working set 5 GB > L2"},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+                "precision": args.precision}
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,136 @@
+/*
+ * msgpu.h -- C ABI of the GB300 Foldy-Lax engine (libmsgpu.so).
+ *
+ * Plain C types only: no torch, no CUDA types in the signatures (streams are
+ * passed as void*).  Complex numbers are two doubles {re, im}, the layout of
+ * C99 `double _Complex` and LAPACK COMPLEX*16.  Matrices are column-major.
+ *
+ * Two layers:
+ *   1. Batched entry points (msgpu_*): the performance path.  Each replaces
+ *      a driver loop of the reference, cited below.
+ *   2. Symbol-compatible drop-ins for the reference's own functions
+ *      (build_ms_matrix, tracelog_lu, dk_log_det_ms, ...) in msgpu_dropin.h.
+ *
+ * Errors: functions return 0 on success, a negative MSGPU_E* code on a usage
+ * or CUDA error (text in msgpu_last_error()).  Numerical conditions are
+ * reported per result in a status word (MSGPU_S*), never by aborting.
+ */
+#ifndef MSGPU_H
+#define MSGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Scattering models, enum order of reference src/core/scattering_model_type.h:241 */
+enum { MSGPU_HARDSPHERE = 0, MSGPU_SOFTSPHERE = 1, MSGPU_RESONANT = 2, MSGPU_MAXIMUM = 3 };
+/* Medium shapes, enum order of reference src/core/medium_type.h:37 */
+enum { MSGPU_CUBE = 0, MSGPU_BALL = 1, MSGPU_LATTICE = 2, MSGPU_GAUSSIAN = 3 };
+/* Arithmetic of the LU */
+enum { MSGPU_FP64 = 0, MSGPU_MIXED = 1 };
+
+/* per-result status bits */
+#define MSGPU_S_OK 0
+#define MSGPU_S_SINGULAR 1  /* an exactly-zero pivot (LAPACK info > 0), ln det = -inf */
+#define MSGPU_S_NONFINITE 2 /* NaN or Inf reached the result */
+
+/* error codes */
+#define MSGPU_E_ARG (-1)
+#define MSGPU_E_CUDA (-2)
+#define MSGPU_E_NODEV (-3)
+#define MSGPU_E_SIZE (-4)
+
+/* Inverse single-atom amplitude model (reference ScatteringModel,
+ * src/core/scattering_model_type.h:246-258, parameters only). */
+typedef struct msgpu_model {
+    int type;     /* MSGPU_MAXIMUM, ... */
+    int np;       /* parameters used */
+    double p[2];  /* hardsphere/softsphere: alpha; resonant: Re p, Im p */
+} msgpu_model;
+
+/* One scatterer set (reference Medium, src/core/medium_type.h:42-54):
+ * d coordinates per atom, n atoms, pos[i*d + c] atom-major, host memory. */
+typedef struct msgpu_medium {
+    int d;
+    int n;
+    const double* pos;
+    msgpu_model model;
+} msgpu_medium;
+
+/* ---- runtime ------------------------------------------------------------ */
+int msgpu_init(int device);               /* select and warm up the device */
+const char* msgpu_last_error(void);
+int msgpu_sm_count(void);
+/* number of kernels this library has launched since load (all entry points) */
+uint64_t msgpu_launch_count(void);
+/* measured FP64 FMA throughput of the device in TFLOP/s (roofline denominator of the FP64 path) */
+int msgpu_probe_fp64(double* tflops);
+
+/* ---- host-side inputs (bit-exact with the reference) -------------------- */
+/* fill_medium (src/core/medium_util.c:164): seeded scatterers, pos[n*d] */
+int msgpu_fill_medium(int d, int n, int shape, double ratio, uint64_t seed, double* pos);
+/* get_arg_cmap (src/core/complex_map_util.c:27) for l = 0..nx*ny-1 */
+void msgpu_kplane_args(int nx, int ny, double xmin, double xmax, double ymin, double ymax, double* ks);
+/* get_arg_ccut (src/core/complex_cut_util.c:32) for l = 0..3(ns+2)-1 */
+void msgpu_kcut_args(int ns, const double* zmin, const double* zmax, double* ks);
+/* set_halton_points (src/core/domain_util.c:180); dom = {xmin,xmax,ymin,ymax} */
+void msgpu_halton_points(const double* dom, int n, double* z);
+
+/* ---- device special functions (check against the reference goldens) ---- */
+/* which: 0 = G_d(k,r) (free_green, src/core/green_bessel.c:280),
+ *        1 = dG/dk (dk_free_green, :311), 2 = I_d(k,r) (free_green_imag, :298),
+ *        3 = K_{d/2}(k) (bessel_k with twonu = d, :224; r ignored),
+ *        4 = F(k)^-1 of *model (invf, src/core/medium_util.c:296; r ignored) */
+int msgpu_eval_special(int which, int d, const msgpu_model* model, int n, const double* ks, const double* rs,
+                       double* out);
+
+/* ---- matrices ----------------------------------------------------------- */
+/* build_ms_matrix / build_dk_ms_matrix (src/core/ms_matrix_util.c:32, :68):
+ * writes the n*n column-major matrix to host memory `mat`. */
+int msgpu_build_matrix(const msgpu_medium* med, const double* k, int deriv, double* mat);
+/* tracelog_lu (src/core/ms_matrix_util.c:185) of a host matrix: out = ln det / n
+ * with the reference's branch (sum of Arg U_ii, + i pi for odd interchanges).
+ * info (may be NULL) = LAPACK zgetrf info: 0, or the 1-based index of the
+ * first exactly-zero pivot. */
+int msgpu_tracelog_matrix(int n, const double* mat, double* out, int* info);
+
+/* ---- batched hot path --------------------------------------------------- */
+/* ln det M(k)/n for nitem items (medium item_med[i], wave number ks[2i..]).
+ * Replaces the k-point loop of run_tracelog_omp (src/core/ms_core.c:115-136)
+ * and build_ms_matrix + tracelog_lu per point.  Host pointers, synchronous.
+ * out[2*nitem], status[nitem] (may be NULL). */
+int msgpu_tracelog_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                         double* out, int* status, int precision);
+/* dlogf = tr(M^-1 dM/dk) (dk_log_det_ms, src/core/ms_matrix_util.c:242) for each item. */
+int msgpu_dk_log_det_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                           double* out, int* status, int precision);
+
+/* Scattering amplitudes a = M^-1 phi for a plane wave along +x, phi_i =
+ * exp(i k x_i) (reference ms_core.c:616-620 zgesv, incident_wave_util.c:76),
+ * and the optical-theorem cross section -Im(conj(phi).a)/k in out[2i]
+ * (total_cross_section, src/core/ms_matrix_util.c:344; out[2i+1] is its
+ * imaginary part for complex k).  amps (may be NULL) receives a for every
+ * item, n_i complex values each, concatenated in item order. */
+int msgpu_amplitude_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                          double* out, double* amps, int* status, int precision);
+
+/* Resident jobs: inputs uploaded once, the hot path run on device-resident
+ * data (asynchronously on `stream`, a cudaStream_t or NULL), results fetched
+ * separately.  kind: 0 = ln det / n, 1 = dlogf, 2 = amplitudes (as above). */
+typedef struct msgpu_job msgpu_job;
+msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
+                            const double* ks, int precision);
+int msgpu_job_run(msgpu_job* job, void* stream);
+int msgpu_job_results(msgpu_job* job, double* out, int* status);
+int msgpu_job_amplitudes(msgpu_job* job, double* amps);
+/* kernels launched by one msgpu_job_run */
+int msgpu_job_launches(const msgpu_job* job);
+/* algorithmic real flops of one msgpu_job_run (8/3 n^3 per ln det; 8/3 n^3 + 8 n^3 per dlogf) */
+double msgpu_job_flops(const msgpu_job* job);
+void msgpu_job_destroy(msgpu_job* job);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,74 @@
+/*
+ * msgpu_dropin.h -- symbol-compatible replacements for the reference's own
+ * hot-path functions.  libmsgpu.so exports these names with the reference's
+ * signatures, so the reference's callers (src/core/ms_core.c, root_finder.c
+ * users, the tests) relink against the GPU without source changes.
+ *
+ * The structs below are layout-identical to the reference types they stand
+ * for; only the fields the hot path reads are named meaningfully.
+ */
+#ifndef MSGPU_DROPIN_H
+#define MSGPU_DROPIN_H
+#include <complex.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef double _Complex msgpu_dcomplex; /* reference dcomplex, src/core/dcomplex_type.h:16 */
+
+/* reference ScatteringModel, src/core/scattering_model_type.h:246-258 */
+typedef struct msgpu_ref_scmodel {
+    int type;
+    int np;
+    double* p;
+    char dir[50];
+    char name[150];
+    char param_ascii[150];
+    char param_latex[150];
+} msgpu_ref_scmodel;
+
+/* reference Medium, src/core/medium_type.h:42-54 */
+typedef struct msgpu_ref_medium {
+    int d;
+    int n;
+    int ntot;
+    int shape;
+    double ratio;
+    msgpu_ref_scmodel* scmodel;
+    double alpha;
+    void* rnd;
+    double* pos;
+} msgpu_ref_medium;
+
+/* reference ComplexData, src/core/complex_data_type.h:17-24 */
+typedef struct msgpu_ref_cdata {
+    int ntot;
+    int nseed;
+    msgpu_dcomplex* data;
+    char title[80];
+    double realtime;
+    msgpu_dcomplex (*get_arg)(void* self, int i);
+} msgpu_ref_cdata;
+
+/* replaces build_ms_matrix, src/core/ms_matrix_util.c:32 */
+void build_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix);
+/* replaces build_dk_ms_matrix, src/core/ms_matrix_util.c:68 */
+void build_dk_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix);
+/* replaces build_plane_wave, src/core/ms_matrix_util.c:88 (host arithmetic) */
+void build_plane_wave(msgpu_ref_medium* med, msgpu_dcomplex k, double theta, msgpu_dcomplex* vec);
+/* replaces tracelog_lu, src/core/ms_matrix_util.c:185; `matrix` is left intact */
+msgpu_dcomplex tracelog_lu(int n, msgpu_dcomplex* matrix);
+/* replaces dk_log_det_ms, src/core/ms_matrix_util.c:242 */
+msgpu_dcomplex dk_log_det_ms(msgpu_ref_medium* med, msgpu_dcomplex k);
+/* replaces total_cross_section, src/core/ms_matrix_util.c:344 */
+double total_cross_section(msgpu_ref_medium* med, double k);
+/* replaces run_tracelog_omp, src/core/ms_core.c:96: every (seed, k) of the
+ * task in one batched GPU job; the seeds are filled with the reference's
+ * generator (seed s = 1..nseed), data[] is the same running average. */
+void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

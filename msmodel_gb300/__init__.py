@@ -1,0 +1,15 @@
+"""msmodel_gb300 -- GB300-native Foldy-Lax hot path of MSModel.
+
+The compute path is libmsgpu.so (hand-written CUDA for sm_103a behind the C
+ABI in include/msgpu.h); this package is the Python host mirror of the
+reference's interface over it.
+"""
+from .api import *  # noqa: F401,F403
+from .api import MsgpuError, lib  # noqa: F401
+
+__all__ = [
+    "Medium", "fill_medium", "kplane_args", "kcut_args", "halton_points", "free_green", "dk_free_green",
+    "free_green_imag", "bessel_k", "invf", "build_ms_matrix", "build_dk_ms_matrix", "tracelog_lu",
+    "tracelog_batch", "dk_log_det_batch", "amplitude_batch", "dk_log_det_ms", "total_cross_section",
+    "run_tracelog", "Job", "init", "launch_count", "sm_count", "MsgpuError", "lib",
+]

@@ -1,0 +1,373 @@
+"""Python host mirror of MSModel's hot-path interface over libmsgpu.so.
+
+Names follow the reference (src/core/ms_matrix_util.h, medium_util.h,
+ms_core.c): ``Medium``/``fill_medium``, ``build_ms_matrix``, ``tracelog_lu``,
+``dk_log_det_ms``, ``total_cross_section``, ``run_tracelog`` (the k-point
+loop of run_tracelog_omp) and their batched forms.  Every numerical call
+goes through the C ABI declared in include/msgpu.h; there is no CPU path:
+if the CUDA library is missing or no GPU is present the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmsgpu.so")
+
+MODELS = {"hardsphere": 0, "softsphere": 1, "resonant": 2, "maximum": 3}
+SHAPES = {"cube": 0, "ball": 1, "lattice": 2, "gaussian": 3}
+PRECISION = {"fp64": 0, "mixed": 1}
+S_SINGULAR, S_NONFINITE = 1, 2
+
+
+class MsgpuError(RuntimeError):
+    pass
+
+
+class _Model(C.Structure):
+    _fields_ = [("type", C.c_int), ("np", C.c_int), ("p", C.c_double * 2)]
+
+
+class _Medium(C.Structure):
+    _fields_ = [("d", C.c_int), ("n", C.c_int), ("pos", C.POINTER(C.c_double)), ("model", _Model)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def lib():
+    """Load libmsgpu.so (built by __graft_entry__.build() / msmodel_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MsgpuError("libmsgpu.so is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    L.msgpu_init.argtypes = [C.c_int]
+    L.msgpu_last_error.restype = C.c_char_p
+    L.msgpu_launch_count.restype = C.c_uint64
+    L.msgpu_probe_fp64.argtypes = [C.POINTER(C.c_double)]
+    L.msgpu_fill_medium.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, _dp]
+    L.msgpu_kplane_args.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
+    L.msgpu_kcut_args.argtypes = [C.c_int, _dp, _dp, _dp]
+    L.msgpu_halton_points.argtypes = [_dp, C.c_int, _dp]
+    L.msgpu_eval_special.argtypes = [C.c_int, C.c_int, C.POINTER(_Model), C.c_int, _dp, C.c_void_p, _dp]
+    L.msgpu_build_matrix.argtypes = [C.POINTER(_Medium), _dp, C.c_int, _dp]
+    L.msgpu_tracelog_matrix.argtypes = [C.c_int, _dp, _dp, C.POINTER(C.c_int)]
+    batch = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip, C.c_int]
+    L.msgpu_tracelog_batch.argtypes = batch
+    L.msgpu_dk_log_det_batch.argtypes = batch
+    L.msgpu_amplitude_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, C.c_void_p, _ip,
+                                        C.c_int]
+    L.msgpu_job_create.restype = C.c_void_p
+    L.msgpu_job_create.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, C.c_int]
+    L.msgpu_job_run.argtypes = [C.c_void_p, C.c_void_p]
+    L.msgpu_job_results.argtypes = [C.c_void_p, _dp, _ip]
+    L.msgpu_job_amplitudes.argtypes = [C.c_void_p, _dp]
+    L.msgpu_job_launches.argtypes = [C.c_void_p]
+    L.msgpu_job_flops.argtypes = [C.c_void_p]
+    L.msgpu_job_flops.restype = C.c_double
+    L.msgpu_job_destroy.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise MsgpuError(f"{what} failed ({rc}): {lib().msgpu_last_error().decode()}")
+
+
+def init(device=0):
+    _check(lib().msgpu_init(device), "msgpu_init")
+
+
+def launch_count():
+    """Kernels launched by libmsgpu.so since it was loaded."""
+    return int(lib().msgpu_launch_count())
+
+
+def probe_fp64_tflops():
+    """Measured FP64 FMA throughput (TFLOP/s) of the current device."""
+    v = C.c_double(0.0)
+    _check(lib().msgpu_probe_fp64(C.byref(v)), "probe_fp64")
+    return v.value
+
+
+def sm_count():
+    return int(lib().msgpu_sm_count())
+
+
+def _model(model="maximum", params=()):
+    m = _Model()
+    m.type = MODELS[model] if isinstance(model, str) else int(model)
+    m.np = len(params)
+    for i, v in enumerate(params):
+        m.p[i] = float(v)
+    return m
+
+
+def _c2(z):
+    z = complex(z)
+    return np.array([z.real, z.imag], dtype=np.float64)
+
+
+def _cplx(zs):
+    zs = np.ascontiguousarray(np.atleast_1d(np.asarray(zs, dtype=np.complex128)))
+    return zs.view(np.float64).reshape(-1).copy()
+
+
+# --------------------------------------------------------------------------- media
+def fill_medium(d, n, seed, shape="ball", ratio=1.0):
+    """Seeded scatterers, bit-exact with the reference fill_medium (medium_util.c:164)."""
+    pos = np.zeros(n * d)
+    _check(lib().msgpu_fill_medium(d, n, SHAPES[shape] if isinstance(shape, str) else shape, ratio, seed, pos),
+           "fill_medium")
+    return pos
+
+
+class Medium:
+    """A scatterer set: d, n, atom-major positions and the scattering model
+    (the reference Medium, src/core/medium_type.h:42-54)."""
+
+    def __init__(self, d, n, pos=None, model="maximum", params=(), shape="ball", ratio=1.0, seed=None):
+        self.d, self.n = int(d), int(n)
+        self.model, self.params, self.shape, self.ratio = model, tuple(params), shape, ratio
+        self.seed = seed
+        if pos is None:
+            pos = fill_medium(d, n, 1 if seed is None else seed, shape, ratio)
+        self.pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        assert self.pos.size == self.n * self.d
+
+    def fill(self, seed):
+        """fill_medium(med, seed): redraw the positions with the given seed."""
+        self.seed = seed
+        self.pos = fill_medium(self.d, self.n, seed, self.shape, self.ratio)
+        return self
+
+    def _struct(self):
+        m = _Medium()
+        m.d, m.n = self.d, self.n
+        m.pos = self.pos.ctypes.data_as(C.POINTER(C.c_double))
+        m.model = _model(self.model, self.params)
+        return m
+
+
+def _media_array(media):
+    arr = (_Medium * len(media))()
+    for i, m in enumerate(media):
+        arr[i] = m._struct()
+    return arr
+
+
+# --------------------------------------------------------------------------- grids
+def kplane_args(nx, ny, xmin, xmax, ymin, ymax):
+    """k of every pixel of a complex map, get_arg_cmap order (complex_map_util.c:27)."""
+    out = np.zeros(2 * nx * ny)
+    lib().msgpu_kplane_args(nx, ny, xmin, xmax, ymin, ymax, out)
+    return out.view(np.complex128).copy()
+
+
+def kcut_args(ns, zmin, zmax):
+    """k of every sample of a complex cut, get_arg_ccut order (complex_cut_util.c:32)."""
+    out = np.zeros(2 * 3 * (ns + 2))
+    lib().msgpu_kcut_args(ns, _c2(zmin), _c2(zmax), out)
+    return out.view(np.complex128).copy()
+
+
+def halton_points(dom, n):
+    """First n Halton (2,3) points of dom = (xmin, xmax, ymin, ymax) (domain_util.c:180)."""
+    out = np.zeros(2 * n)
+    lib().msgpu_halton_points(np.asarray(dom, dtype=np.float64), n, out)
+    return out.view(np.complex128).copy()
+
+
+# --------------------------------------------------------------------------- device special functions
+def eval_special(which, d, ks, rs=None, model="maximum", params=()):
+    kk = _cplx(ks)
+    n = kk.size // 2
+    out = np.zeros(2 * n)
+    m = _model(model, params)
+    rr = None if rs is None else np.ascontiguousarray(np.broadcast_to(np.asarray(rs, dtype=np.float64), (n,)))
+    _check(lib().msgpu_eval_special(which, d, C.byref(m), n, kk, None if rr is None else rr.ctypes.data, out),
+           "eval_special")
+    return out.view(np.complex128).copy()
+
+
+def free_green(d, ks, rs=1.0):
+    return eval_special(0, d, ks, rs)
+
+
+def dk_free_green(d, ks, rs=1.0):
+    return eval_special(1, d, ks, rs)
+
+
+def free_green_imag(d, ks, rs=1.0):
+    return eval_special(2, d, ks, rs)
+
+
+def bessel_k(twonu, zs):
+    return eval_special(3, twonu, zs)
+
+
+def invf(d, ks, model="maximum", params=()):
+    return eval_special(4, d, ks, None, model, params)
+
+
+# --------------------------------------------------------------------------- single matrices
+def build_ms_matrix(med, k, deriv=False):
+    """M(k) (or dM/dk) assembled on the GPU; returned as an [row, col] array."""
+    out = np.zeros(2 * med.n * med.n)
+    s = med._struct()
+    _check(lib().msgpu_build_matrix(C.byref(s), _c2(k), int(deriv), out), "build_ms_matrix")
+    return out.view(np.complex128).reshape(med.n, med.n).T
+
+
+def build_dk_ms_matrix(med, k):
+    return build_ms_matrix(med, k, deriv=True)
+
+
+def tracelog_lu(matrix):
+    """ln det(M)/n of an [row, col] matrix, LU on the GPU (ms_matrix_util.c:185). Returns (value, info)."""
+    a = np.asarray(matrix, dtype=np.complex128)
+    n = a.shape[0]
+    buf = np.ascontiguousarray(a.T).view(np.float64).reshape(-1).copy()
+    out = np.zeros(2)
+    info = C.c_int(0)
+    _check(lib().msgpu_tracelog_matrix(n, buf, out, C.byref(info)), "tracelog_lu")
+    return complex(out[0], out[1]), info.value
+
+
+# --------------------------------------------------------------------------- batches
+def _items(media, ks, item_med):
+    kk = _cplx(ks)
+    nitem = kk.size // 2
+    if item_med is None:
+        im = np.zeros(nitem, dtype=np.int32)
+    else:
+        im = np.ascontiguousarray(item_med, dtype=np.int32)
+    assert im.size == nitem
+    return kk, nitem, im
+
+
+def tracelog_batch(media, ks, item_med=None, precision="fp64"):
+    """ln det M(k)/n for every item (medium item_med[i], wave number ks[i])."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    kk, nitem, im = _items(media, ks, item_med)
+    out = np.zeros(2 * nitem)
+    st = np.zeros(nitem, dtype=np.int32)
+    arr = _media_array(media)
+    _check(lib().msgpu_tracelog_batch(len(media), arr, nitem, im, kk, out, st, PRECISION[precision]),
+           "tracelog_batch")
+    return out.view(np.complex128).copy(), st
+
+
+def dk_log_det_batch(media, ks, item_med=None, precision="fp64"):
+    """tr(M^-1 dM/dk) for every item (dk_log_det_ms, ms_matrix_util.c:242)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    kk, nitem, im = _items(media, ks, item_med)
+    out = np.zeros(2 * nitem)
+    st = np.zeros(nitem, dtype=np.int32)
+    arr = _media_array(media)
+    _check(lib().msgpu_dk_log_det_batch(len(media), arr, nitem, im, kk, out, st, PRECISION[precision]),
+           "dk_log_det_batch")
+    return out.view(np.complex128).copy(), st
+
+
+def amplitude_batch(media, ks, item_med=None, precision="fp64", want_amps=True):
+    """a = M^-1 phi (plane wave along +x) and -Im(conj(phi).a)/k per item."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    kk, nitem, im = _items(media, ks, item_med)
+    out = np.zeros(2 * nitem)
+    st = np.zeros(nitem, dtype=np.int32)
+    ntot = sum(media[i].n for i in im)
+    amps = np.zeros(2 * ntot) if want_amps else None
+    arr = _media_array(media)
+    _check(lib().msgpu_amplitude_batch(len(media), arr, nitem, im, kk, out,
+                                       None if amps is None else amps.ctypes.data, st, PRECISION[precision]),
+           "amplitude_batch")
+    sig = out.view(np.complex128).copy()
+    if amps is None:
+        return sig, None, st
+    amps = amps.view(np.complex128)
+    parts, off = [], 0
+    for i in im:
+        parts.append(amps[off:off + media[i].n].copy())
+        off += media[i].n
+    return sig, parts, st
+
+
+def dk_log_det_ms(med, k):
+    """Scalar form of dk_log_det_ms (ms_matrix_util.c:242)."""
+    v, st = dk_log_det_batch([med], [k])
+    return complex(v[0])
+
+
+def total_cross_section(med, k):
+    """Optical-theorem total cross section at real k (ms_matrix_util.c:344)."""
+    sig, _, _ = amplitude_batch([med], [k], want_amps=False)
+    return float(sig[0].real)
+
+
+def run_tracelog(d, n, ks, nseed=1, model="maximum", params=(), shape="ball", ratio=1.0, precision="fp64"):
+    """The k-point loop of run_tracelog_omp (ms_core.c:96-141): seeds 1..nseed,
+    ln det/n at every k, averaged over seeds in seed order."""
+    media = [Medium(d, n, model=model, params=params, shape=shape, ratio=ratio, seed=s) for s in range(1, nseed + 1)]
+    ks = np.atleast_1d(np.asarray(ks, dtype=np.complex128))
+    nk = ks.size
+    allk = np.tile(ks, nseed)
+    im = np.repeat(np.arange(nseed, dtype=np.int32), nk)
+    out, st = tracelog_batch(media, allk, im, precision)
+    data = np.zeros(nk, dtype=np.complex128)
+    for s in range(1, nseed + 1):
+        data = ((s - 1) * data + out[(s - 1) * nk:s * nk]) / s
+    return data, st
+
+
+class Job:
+    """A resident job: inputs on the device, run asynchronously on a stream
+    (the handle of a CUDA stream, e.g. torch.cuda.current_stream().cuda_stream)."""
+
+    KINDS = {"tracelog": 0, "dlogf": 1, "amplitude": 2}
+
+    def __init__(self, kind, media, ks, item_med=None, precision="fp64"):
+        media = [media] if isinstance(media, Medium) else list(media)
+        self.media = media
+        kk, self.nitem, im = _items(media, ks, item_med)
+        self._keep = (kk, im)
+        arr = _media_array(media)
+        self.kind = self.KINDS[kind]
+        self.h = lib().msgpu_job_create(self.kind, len(media), arr, self.nitem, im, kk, PRECISION[precision])
+        if not self.h:
+            raise MsgpuError("job_create failed: " + lib().msgpu_last_error().decode())
+        self.item_med = im
+
+    def run(self, stream=None):
+        _check(lib().msgpu_job_run(self.h, stream), "job_run")
+
+    def results(self):
+        out = np.zeros(2 * self.nitem)
+        st = np.zeros(self.nitem, dtype=np.int32)
+        _check(lib().msgpu_job_results(self.h, out, st), "job_results")
+        return out.view(np.complex128).copy(), st
+
+    @property
+    def flops(self):
+        return float(lib().msgpu_job_flops(self.h))
+
+    @property
+    def launches(self):
+        return int(lib().msgpu_job_launches(self.h))
+
+    def close(self):
+        if self.h:
+            lib().msgpu_job_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,140 @@
+/*
+ * dropin.c -- the reference's hot-path symbols over the GPU engine.
+ *
+ * Compiled as C so that `double _Complex` arguments and return values follow
+ * the platform ABI exactly as the reference's callers expect.  Each function
+ * keeps its reference counterpart's meaning: matrices are caller-allocated,
+ * column-major n*n; LAPACK warnings are printed in the reference's words
+ * (src/core/ms_matrix_util.c:188-190, :250-252, :358-360).
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "msgpu.h"
+#include "msgpu_dropin.h"
+
+static msgpu_model to_model(const msgpu_ref_scmodel* sm) {
+    msgpu_model m;
+    memset(&m, 0, sizeof(m));
+    m.type = sm->type;
+    m.np = sm->np < 2 ? sm->np : 2;
+    for (int i = 0; i < m.np; i++) m.p[i] = sm->p[i];
+    return m;
+}
+
+static msgpu_medium to_medium(const msgpu_ref_medium* med) {
+    msgpu_medium m;
+    m.d = med->d;
+    m.n = med->n;
+    m.pos = med->pos;
+    m.model = to_model(med->scmodel);
+    return m;
+}
+
+static void fail(const char* where, int e) {
+    fprintf(stderr, "[ERROR] %s: GPU call failed (%d): %s\n", where, e, msgpu_last_error());
+    exit(EXIT_FAILURE);
+}
+
+void build_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix) {
+    msgpu_medium m = to_medium(med);
+    double kk[2] = {creal(k), cimag(k)};
+    int e = msgpu_build_matrix(&m, kk, 0, (double*)matrix);
+    if (e) fail("build_ms_matrix", e);
+}
+
+void build_dk_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix) {
+    msgpu_medium m = to_medium(med);
+    double kk[2] = {creal(k), cimag(k)};
+    int e = msgpu_build_matrix(&m, kk, 1, (double*)matrix);
+    if (e) fail("build_dk_ms_matrix", e);
+}
+
+/* host arithmetic, as the reference: phi_i = exp(i k (cos t x_i + sin t y_i)) */
+void build_plane_wave(msgpu_ref_medium* med, msgpu_dcomplex k, double theta, msgpu_dcomplex* vec) {
+    const int d = med->d, n = med->n;
+    theta *= 3.1415926535897932385 / 180;
+    double ct = cos(theta), st = sin(theta);
+    if (d == 1) {
+        ct = ct > 0. ? 1. : -1.;
+        for (int i = 0; i < n; i++) vec[i] = cexp(I * k * ct * med->pos[i]);
+    } else {
+        for (int i = 0; i < n; i++) vec[i] = cexp(I * k * (ct * med->pos[i * d] + st * med->pos[i * d + 1]));
+    }
+}
+
+msgpu_dcomplex tracelog_lu(int n, msgpu_dcomplex* matrix) {
+    double out[2];
+    int info = 0;
+    int e = msgpu_tracelog_matrix(n, (const double*)matrix, out, &info);
+    if (e) fail("tracelog_lu", e);
+    if (info > 0) printf("[LAPACK] Element U(%d,%d) is exactly zero, the determinant will be singular.\n", info, info);
+    return out[0] + I * out[1];
+}
+
+msgpu_dcomplex dk_log_det_ms(msgpu_ref_medium* med, msgpu_dcomplex k) {
+    msgpu_medium m = to_medium(med);
+    double kk[2] = {creal(k), cimag(k)}, out[2];
+    int st = 0;
+    int e = msgpu_dk_log_det_batch(1, &m, 1, NULL, kk, out, &st, MSGPU_FP64);
+    if (e) fail("dk_log_det_ms", e);
+    if (st & MSGPU_S_SINGULAR) printf("[LAPACK] Element U(i,i) is exactly zero, the inverse matrix will be singular.\n");
+    return out[0] + I * out[1];
+}
+
+double total_cross_section(msgpu_ref_medium* med, double k) {
+    msgpu_medium m = to_medium(med);
+    double kk[2] = {k, 0.0}, out[2];
+    int st = 0;
+    int e = msgpu_amplitude_batch(1, &m, 1, NULL, kk, out, NULL, &st, MSGPU_FP64);
+    if (e) fail("total_cross_section", e);
+    if (st & MSGPU_S_SINGULAR) printf("[LAPACK] Element U(i,i) is exactly zero, the solution could not be computed.\n");
+    return out[0];
+}
+
+void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread) {
+    (void)nthread;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int d = med->d, n = med->n, nseed = cdata->nseed, ntot = cdata->ntot;
+    msgpu_medium* media = (msgpu_medium*)calloc((size_t)nseed, sizeof(msgpu_medium));
+    double* pos = (double*)malloc(sizeof(double) * (size_t)nseed * n * d);
+    double* ks = (double*)malloc(sizeof(double) * 2 * (size_t)nseed * ntot);
+    int* im = (int*)malloc(sizeof(int) * (size_t)nseed * ntot);
+    double* out = (double*)malloc(sizeof(double) * 2 * (size_t)nseed * ntot);
+    msgpu_model mdl = to_model(med->scmodel);
+    for (int s = 0; s < nseed; s++) {
+        double* p = pos + (size_t)s * n * d;
+        int e = msgpu_fill_medium(d, n, med->shape, med->ratio, (uint64_t)(s + 1), p);
+        if (e) fail("run_tracelog_omp: fill_medium", e);
+        media[s].d = d;
+        media[s].n = n;
+        media[s].pos = p;
+        media[s].model = mdl;
+        for (int l = 0; l < ntot; l++) {
+            msgpu_dcomplex k = cdata->get_arg(cdata, l);
+            size_t it = (size_t)s * ntot + l;
+            ks[2 * it] = creal(k);
+            ks[2 * it + 1] = cimag(k);
+            im[it] = s;
+        }
+    }
+    int e = msgpu_tracelog_batch(nseed, media, nseed * ntot, im, ks, out, NULL, MSGPU_FP64);
+    if (e) fail("run_tracelog_omp", e);
+    /* running average over seeds in seed order (ms_core.c:127) */
+    for (int s = 1; s <= nseed; s++)
+        for (int l = 0; l < ntot; l++) {
+            size_t it = (size_t)(s - 1) * ntot + l;
+            msgpu_dcomplex t = out[2 * it] + I * out[2 * it + 1];
+            cdata->data[l] = ((s - 1) * cdata->data[l] + t) / s;
+        }
+    /* leave the medium filled with the last seed, as the reference loop does */
+    if (nseed > 0) memcpy(med->pos, pos + (size_t)(nseed - 1) * n * d, sizeof(double) * (size_t)n * d);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    cdata->realtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+    free(media); free(pos); free(ks); free(im); free(out);
+}

@@ -1,0 +1,581 @@
+// engine.cu -- batched Foldy-Lax engine: persistent kernels over a device
+// work queue, the runtime (device, workspace, jobs) and the msgpu_* C ABI.
+//
+// One CTA takes the next (k, realisation) item from an atomic counter,
+// assembles M(k) (and dM/dk) into its private slot of the workspace, factors
+// it and reduces the trace-log or the trace of M^-1 dM/dk, then takes the
+// next item.  Items are dealt largest-n first, so uneven sizes balance.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "msgpu.h"
+#include "lu64.cuh"
+#include "engine_internal.h"
+
+using namespace msg;
+
+namespace msg {
+
+// complex elements of one CTA slot: the matrix, plus dM/dk (kind 1) or the
+// right-hand side (kind 2)
+__host__ __device__ inline size_t slot_elems(int kind, size_t slot, int nmax) {
+    if (kind == 1) return 2 * slot;
+    if (kind == 2) return slot + (((size_t)nmax + 15) / 16) * 16;
+    return slot;
+}
+
+__global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LuSmem& s = *reinterpret_cast<LuSmem*>(smem_raw);
+    zc* A = P.ws + (size_t)blockIdx.x * slot_elems(P.kind, P.slot, P.piv_stride);
+    zc* B = (P.kind >= 1) ? A + P.slot : nullptr;
+    int* ipiv = P.piv + (size_t)blockIdx.x * P.piv_stride;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s.item = (int)atomicAdd(P.counter, 1u);
+            s.info = 0;
+        }
+        __syncthreads();
+        const int q = s.item;
+        if (q >= P.nitem) break;
+        const int it = P.order[q];
+        const MedDev md = P.media[P.item_med[it]];
+        const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
+        assemble(A, P.kind == 1 ? B : nullptr, md.n, md.d, md.pos, md.model, k, s);
+        zc res;
+        if (P.kind == 2) {
+            // incident plane wave along +x (reference incident_wave_util.c:76, ms_core.c:616-618)
+            for (int i = threadIdx.x; i < md.n; i += NT) B[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
+            __syncthreads();
+        }
+        lu_factor(A, md.n, ipiv, s);
+        if (P.kind == 0) {
+            res = lu_tracelog(A, md.n, ipiv, s);
+        } else if (P.kind == 1) {
+            res = lu_trace_solve(A, B, md.n, ipiv, s);
+        } else {
+            lu_solve_vec(A, B, md.n, ipiv, s);
+            // optical theorem sigma = -Im(conj(phi).a)/k (reference ms_matrix_util.c:361)
+            double dr = 0.0, di = 0.0, z = 0.0;
+            for (int i = threadIdx.x; i < md.n; i += NT) {
+                zc ph = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
+                zc t = conjz(ph) * B[i];
+                dr += t.re;
+                di += t.im;
+                if (P.amps) {
+                    P.amps[2 * (P.amp_off[it] + i)] = B[i].re;
+                    P.amps[2 * (P.amp_off[it] + i) + 1] = B[i].im;
+                }
+            }
+            block_sum3(dr, di, z, s);
+            res = mk(-di, 0.0) / k;
+        }
+        if (threadIdx.x == 0) {
+            P.out[2 * it] = res.re;
+            P.out[2 * it + 1] = res.im;
+            int st = 0;
+            if (s.info) st |= MSGPU_S_SINGULAR;
+            if (!isfinite(res.re) || !isfinite(res.im)) st |= MSGPU_S_NONFINITE;
+            P.status[it] = st;
+        }
+        __syncthreads();
+    }
+}
+
+// single-matrix kernels used by the drop-in layer ---------------------------------
+__global__ void __launch_bounds__(NT, 1) k_build_matrix(zc* A, int n, int d, const double* pos, msgpu_model m,
+                                                        double kre, double kim, int deriv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LuSmem& s = *reinterpret_cast<LuSmem*>(smem_raw);
+    // a grid of CTAs shares the column tiles: CTA b assembles column tiles J = b, b + grid, ...
+    const int tid = threadIdx.x;
+    const zc k = mk(kre, kim);
+    if (tid == 0) s.diag[0] = deriv ? dk_invf(m, d, k) : invf(m, d, k);
+    __syncthreads();
+    const int nt = (n + 31) / 32;
+    for (int J = blockIdx.x; J < nt; J += gridDim.x) {
+        for (int I = 0; I <= J; ++I) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+                const int i = I * 32 + ii, j = J * 32 + jj;
+                if (i < n && j < n && i <= j) {
+                    zc v;
+                    if (i < j) {
+                        zc mm, dm;
+                        pair_elements(d, k, atom_distance(d, pos, i, j), deriv != 0, mm, dm);
+                        v = deriv ? dm : mm;
+                    } else {
+                        v = s.diag[0];
+                    }
+                    A[i + (size_t)j * n] = v;
+                    s.T[jj][ii] = v;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int jj = tid & 31, ii = (tid >> 5) + 8 * q;
+                const int i = I * 32 + ii, j = J * 32 + jj;
+                if (j < n && i < j) A[j + (size_t)i * n] = s.T[jj][ii];
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NT, 1) k_tracelog_matrix(zc* A, int n, int* ipiv, double* out, int* info) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LuSmem& s = *reinterpret_cast<LuSmem*>(smem_raw);
+    if (threadIdx.x == 0) s.info = 0;
+    __syncthreads();
+    lu_factor(A, n, ipiv, s);
+    zc r = lu_tracelog(A, n, ipiv, s);
+    if (threadIdx.x == 0) {
+        out[0] = r.re;
+        out[1] = r.im;
+        *info = s.info;
+    }
+}
+
+__global__ void k_eval_special(int which, int d, msgpu_model m, int n, const double* ks, const double* rs,
+                               double* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    zc k = mk(ks[2 * i], ks[2 * i + 1]);
+    double r = rs ? rs[i] : 1.0;
+    zc v;
+    switch (which) {
+    case 0: v = free_green(d, k, r); break;
+    case 1: v = dk_free_green(d, k, r); break;
+    case 2: v = free_green_imag(d, k, r); break;
+    case 3: v = bessel_k(d, k); break;
+    default: v = invf(m, d, k); break;
+    }
+    out[2 * i] = v.re;
+    out[2 * i + 1] = v.im;
+}
+
+// FP64 FMA throughput probe: 8 independent chains per thread.  MEASURED_PEAKS
+// carries no FP64 figure, so the plain path's roofline denominator is this.
+__global__ void k_probe_dfma(double* sink, int iters, double a, double b) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+           x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 12345.678) sink[blockIdx.x] = s;
+}
+
+}  // namespace msg
+
+// ---------------------------------------------------------------------------
+// runtime
+// ---------------------------------------------------------------------------
+namespace {
+
+std::mutex g_mu;
+std::string g_err;
+int g_dev = -1;
+int g_sms = 0;
+int g_ctas_fp64 = 0;
+std::atomic<uint64_t> g_launches{0};
+void* g_ws = nullptr;
+size_t g_ws_bytes = 0;
+
+int set_err(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return set_err(MSGPU_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+size_t smem_bytes() { return sizeof(LuSmem); }
+
+int init_locked(int device) {
+    if (g_dev >= 0) return 0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return set_err(MSGPU_E_NODEV, "no CUDA device");
+    if (device < 0) device = 0;
+    CK(cudaSetDevice(device));
+    cudaDeviceProp pr;
+    CK(cudaGetDeviceProperties(&pr, device));
+    g_sms = pr.multiProcessorCount;
+    CK(cudaFuncSetAttribute(k_engine_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes()));
+    CK(cudaFuncSetAttribute(k_build_matrix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes()));
+    CK(cudaFuncSetAttribute(k_tracelog_matrix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes()));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_engine_fp64, NT, smem_bytes()));
+    g_ctas_fp64 = std::max(1, occ);
+    g_dev = device;
+    return 0;
+}
+
+int ensure_ws(size_t bytes, void** p) {
+    if (bytes > g_ws_bytes) {
+        if (g_ws) cudaFree(g_ws);
+        g_ws = nullptr;
+        g_ws_bytes = 0;
+        CK(cudaMalloc(&g_ws, bytes));
+        g_ws_bytes = bytes;
+    }
+    *p = g_ws;
+    return 0;
+}
+
+}  // namespace
+
+// workspace budget for the per-CTA matrix slots
+static size_t ws_budget() {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    size_t cap = (size_t)48 << 30;
+    size_t avail = fr + g_ws_bytes;
+    return std::min(cap, avail > ((size_t)4 << 30) ? avail - ((size_t)4 << 30) : avail / 2);
+}
+
+struct msgpu_job {
+    int kind = 0, precision = 0, nitem = 0, nmed = 0, nmax = 0;
+    double flops = 0.0;
+    int grid = 0;
+    MedDev* d_media = nullptr;
+    double* d_pos = nullptr;
+    double* d_ks = nullptr;
+    int* d_item_med = nullptr;
+    int* d_order = nullptr;
+    double* d_out = nullptr;
+    int* d_status = nullptr;
+    unsigned* d_counter = nullptr;
+    int* d_piv = nullptr;
+    size_t slot = 0;
+    size_t ws_bytes = 0;
+    long long amp_total = 0;
+    double* d_amps = nullptr;
+    long long* d_amp_off = nullptr;
+};
+
+extern "C" {
+
+int msgpu_init(int device) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return init_locked(device);
+}
+
+const char* msgpu_last_error(void) { return g_err.c_str(); }
+
+int msgpu_sm_count(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (init_locked(-1)) return 0;
+    return g_sms;
+}
+
+uint64_t msgpu_launch_count(void) { return g_launches.load(); }
+
+int msgpu_probe_fp64(double* tflops) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (int e = init_locked(-1)) return e;
+    double* sink = nullptr;
+    CK(cudaMalloc(&sink, sizeof(double) * 4096));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int blocks = g_sms * 4, threads = 256, iters = 8192;
+    k_probe_dfma<<<blocks, threads>>>(sink, 64, 0.999999, 1e-7);  // warm-up
+    g_launches++;
+    CK(cudaEventRecord(e0));
+    k_probe_dfma<<<blocks, threads>>>(sink, iters, 0.999999, 1e-7);
+    g_launches++;
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    return 0;
+}
+
+int msgpu_eval_special(int which, int d, const msgpu_model* model, int n, const double* ks, const double* rs,
+                       double* out) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (int e = init_locked(-1)) return e;
+    if (n <= 0) return 0;
+    msgpu_model m{};
+    if (model) m = *model;
+    double *dk = nullptr, *dr = nullptr, *dout = nullptr;
+    CK(cudaMalloc(&dk, sizeof(double) * 2 * n));
+    CK(cudaMalloc(&dout, sizeof(double) * 2 * n));
+    if (rs) CK(cudaMalloc(&dr, sizeof(double) * n));
+    CK(cudaMemcpy(dk, ks, sizeof(double) * 2 * n, cudaMemcpyHostToDevice));
+    if (rs) CK(cudaMemcpy(dr, rs, sizeof(double) * n, cudaMemcpyHostToDevice));
+    k_eval_special<<<(n + 127) / 128, 128>>>(which, d, m, n, dk, dr, dout);
+    g_launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(out, dout, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+    cudaFree(dk);
+    cudaFree(dout);
+    if (dr) cudaFree(dr);
+    return 0;
+}
+
+int msgpu_build_matrix(const msgpu_medium* med, const double* k, int deriv, double* mat) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (int e = init_locked(-1)) return e;
+    if (!med || med->n < 1 || med->d < 1 || !med->pos || !k || !mat) return set_err(MSGPU_E_ARG, "bad argument");
+    const int n = med->n, d = med->d;
+    double* dpos = nullptr;
+    zc* dA = nullptr;
+    CK(cudaMalloc(&dpos, sizeof(double) * (size_t)n * d));
+    CK(cudaMalloc(&dA, sizeof(zc) * (size_t)n * n));
+    CK(cudaMemcpy(dpos, med->pos, sizeof(double) * (size_t)n * d, cudaMemcpyHostToDevice));
+    int nt = (n + 31) / 32;
+    k_build_matrix<<<std::min(nt, 4 * g_sms), NT, smem_bytes()>>>(dA, n, d, dpos, med->model, k[0], k[1], deriv);
+    g_launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(mat, dA, sizeof(zc) * (size_t)n * n, cudaMemcpyDeviceToHost));
+    cudaFree(dpos);
+    cudaFree(dA);
+    return 0;
+}
+
+int msgpu_tracelog_matrix(int n, const double* mat, double* out, int* info) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (int e = init_locked(-1)) return e;
+    if (n < 1 || !mat || !out) return set_err(MSGPU_E_ARG, "bad argument");
+    zc* dA = nullptr;
+    int* dp = nullptr;
+    double* dout = nullptr;
+    CK(cudaMalloc(&dA, sizeof(zc) * (size_t)n * n));
+    CK(cudaMalloc(&dp, sizeof(int) * (size_t)n + 64));
+    CK(cudaMalloc(&dout, 64));
+    CK(cudaMemcpy(dA, mat, sizeof(zc) * (size_t)n * n, cudaMemcpyHostToDevice));
+    k_tracelog_matrix<<<1, NT, smem_bytes()>>>(dA, n, dp, dout, reinterpret_cast<int*>(dout + 2));
+    g_launches++;
+    CK(cudaGetLastError());
+    double h[3];
+    CK(cudaMemcpy(h, dout, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+    out[0] = h[0];
+    out[1] = h[1];
+    if (info) std::memcpy(info, &h[2], sizeof(int));
+    cudaFree(dA);
+    cudaFree(dp);
+    cudaFree(dout);
+    return 0;
+}
+
+msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
+                            const double* ks, int precision) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (init_locked(-1)) return nullptr;
+    if (kind < 0 || kind > 2 || nmed < 1 || !media || nitem < 1 || !ks) {
+        set_err(MSGPU_E_ARG, "job: bad argument");
+        return nullptr;
+    }
+    if (precision != MSGPU_FP64 && precision != MSGPU_MIXED) {
+        set_err(MSGPU_E_ARG, "job: unknown precision");
+        return nullptr;
+    }
+    auto* J = new msgpu_job();
+    J->kind = kind;
+    J->precision = precision;
+    J->nitem = nitem;
+    J->nmed = nmed;
+    std::vector<MedDev> hm(nmed);
+    size_t npos = 0;
+    for (int i = 0; i < nmed; i++) {
+        const msgpu_medium& m = media[i];
+        if (m.n < 1 || m.d < 1 || m.d > 20 || !m.pos || m.n > 50000) {
+            set_err(MSGPU_E_ARG, "job: bad medium");
+            delete J;
+            return nullptr;
+        }
+        J->nmax = std::max(J->nmax, m.n);
+        npos += (size_t)m.n * m.d;
+    }
+    std::vector<int> med_of(nitem);
+    for (int i = 0; i < nitem; i++) {
+        int mi = item_med ? item_med[i] : 0;
+        if (mi < 0 || mi >= nmed) {
+            set_err(MSGPU_E_ARG, "job: bad item medium");
+            delete J;
+            return nullptr;
+        }
+        med_of[i] = mi;
+        double n3 = (double)media[mi].n * media[mi].n * media[mi].n;
+        double n2 = (double)media[mi].n * media[mi].n;
+        J->flops += (kind == 0) ? 8.0 / 3.0 * n3 : (kind == 1 ? (8.0 / 3.0 + 8.0) * n3 : 8.0 / 3.0 * n3 + 8.0 * n2);
+        J->amp_total += media[mi].n;
+    }
+    // largest matrices first
+    std::vector<int> order(nitem);
+    for (int i = 0; i < nitem; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return media[med_of[a]].n > media[med_of[b]].n; });
+    auto fail = [&](const char* what) -> msgpu_job* {
+        set_err(MSGPU_E_CUDA, std::string("job: ") + what);
+        msgpu_job_destroy(J);
+        return nullptr;
+    };
+    if (cudaMalloc(&J->d_media, sizeof(MedDev) * nmed) != cudaSuccess) return fail("alloc media");
+    if (cudaMalloc(&J->d_pos, sizeof(double) * npos) != cudaSuccess) return fail("alloc pos");
+    if (cudaMalloc(&J->d_ks, sizeof(double) * 2 * nitem) != cudaSuccess) return fail("alloc ks");
+    if (cudaMalloc(&J->d_item_med, sizeof(int) * nitem) != cudaSuccess) return fail("alloc items");
+    if (cudaMalloc(&J->d_order, sizeof(int) * nitem) != cudaSuccess) return fail("alloc order");
+    if (cudaMalloc(&J->d_out, sizeof(double) * 2 * nitem) != cudaSuccess) return fail("alloc out");
+    if (cudaMalloc(&J->d_status, sizeof(int) * nitem) != cudaSuccess) return fail("alloc status");
+    if (cudaMalloc(&J->d_counter, 256) != cudaSuccess) return fail("alloc counter");
+    if (kind == 2) {
+        std::vector<long long> off(nitem);
+        long long acc = 0;
+        for (int i = 0; i < nitem; i++) { off[i] = acc; acc += media[med_of[i]].n; }
+        if (cudaMalloc(&J->d_amps, sizeof(double) * 2 * (size_t)acc) != cudaSuccess) return fail("alloc amps");
+        if (cudaMalloc(&J->d_amp_off, sizeof(long long) * nitem) != cudaSuccess) return fail("alloc amp_off");
+        if (cudaMemcpy(J->d_amp_off, off.data(), sizeof(long long) * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail("copy amp_off");
+    }
+    size_t off = 0;
+    for (int i = 0; i < nmed; i++) {
+        const msgpu_medium& m = media[i];
+        size_t cnt = (size_t)m.n * m.d;
+        if (cudaMemcpy(J->d_pos + off, m.pos, sizeof(double) * cnt, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail("copy pos");
+        hm[i] = MedDev{m.d, m.n, J->d_pos + off, m.model};
+        off += cnt;
+    }
+    if (cudaMemcpy(J->d_media, hm.data(), sizeof(MedDev) * nmed, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail("copy media");
+    if (cudaMemcpy(J->d_ks, ks, sizeof(double) * 2 * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail("copy ks");
+    if (cudaMemcpy(J->d_item_med, med_of.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail("copy items");
+    if (cudaMemcpy(J->d_order, order.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail("copy order");
+    // per-CTA slots
+    J->slot = (size_t)J->nmax * J->nmax;
+    const size_t per_cta = slot_elems(kind, J->slot, J->nmax) * sizeof(zc);
+    int grid = std::min(nitem, g_sms * g_ctas_fp64);
+    size_t budget = ws_budget();
+    while (grid > 1 && (size_t)grid * per_cta > budget) grid--;
+    J->grid = grid;
+    J->ws_bytes = (size_t)grid * per_cta;
+    if (cudaMalloc(&J->d_piv, sizeof(int) * (size_t)grid * J->nmax) != cudaSuccess) return fail("alloc piv");
+    void* ws = nullptr;
+    if (ensure_ws(J->ws_bytes, &ws)) {
+        msgpu_job_destroy(J);
+        return nullptr;
+    }
+    return J;
+}
+
+int msgpu_job_run(msgpu_job* J, void* stream) {
+    if (!J) return set_err(MSGPU_E_ARG, "null job");
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    void* ws = nullptr;
+    if (int e = ensure_ws(J->ws_bytes, &ws)) return e;
+    CK(cudaMemsetAsync(J->d_counter, 0, sizeof(unsigned), st));
+    EngineParams P;
+    P.media = J->d_media;
+    P.ks = J->d_ks;
+    P.item_med = J->d_item_med;
+    P.order = J->d_order;
+    P.nitem = J->nitem;
+    P.ws = reinterpret_cast<zc*>(ws);
+    P.slot = J->slot;
+    P.piv = J->d_piv;
+    P.piv_stride = J->nmax;
+    P.out = J->d_out;
+    P.status = J->d_status;
+    P.counter = J->d_counter;
+    P.kind = J->kind;
+    P.amps = J->d_amps;
+    P.amp_off = J->d_amp_off;
+    if (J->precision == MSGPU_MIXED) {
+        int e = mixed_run(P, J->grid, J->nmax, st);
+        g_launches += mixed_launches();
+        return e;
+    }
+    k_engine_fp64<<<J->grid, NT, smem_bytes(), st>>>(P);
+    g_launches++;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int msgpu_job_launches(const msgpu_job* J) { return J ? 1 : 0; }
+double msgpu_job_flops(const msgpu_job* J) { return J ? J->flops : 0.0; }
+
+int msgpu_job_results(msgpu_job* J, double* out, int* status) {
+    if (!J) return set_err(MSGPU_E_ARG, "null job");
+    CK(cudaDeviceSynchronize());
+    if (out) CK(cudaMemcpy(out, J->d_out, sizeof(double) * 2 * J->nitem, cudaMemcpyDeviceToHost));
+    if (status) CK(cudaMemcpy(status, J->d_status, sizeof(int) * J->nitem, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int msgpu_job_amplitudes(msgpu_job* J, double* amps) {
+    if (!J || J->kind != 2 || !amps) return set_err(MSGPU_E_ARG, "job_amplitudes: not an amplitude job");
+    CK(cudaDeviceSynchronize());
+    CK(cudaMemcpy(amps, J->d_amps, sizeof(double) * 2 * (size_t)J->amp_total, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+void msgpu_job_destroy(msgpu_job* J) {
+    if (!J) return;
+    cudaFree(J->d_media);
+    cudaFree(J->d_pos);
+    cudaFree(J->d_ks);
+    cudaFree(J->d_item_med);
+    cudaFree(J->d_order);
+    cudaFree(J->d_out);
+    cudaFree(J->d_status);
+    cudaFree(J->d_counter);
+    cudaFree(J->d_piv);
+    cudaFree(J->d_amps);
+    cudaFree(J->d_amp_off);
+    delete J;
+}
+
+static int run_batch(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                     double* out, int* status, int precision) {
+    msgpu_job* J = msgpu_job_create(kind, nmed, media, nitem, item_med, ks, precision);
+    if (!J) return g_err.empty() ? MSGPU_E_ARG : (g_err.find("CUDA") != std::string::npos ? MSGPU_E_CUDA : MSGPU_E_ARG);
+    int e = msgpu_job_run(J, nullptr);
+    if (!e) e = msgpu_job_results(J, out, status);
+    msgpu_job_destroy(J);
+    return e;
+}
+
+int msgpu_tracelog_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                         double* out, int* status, int precision) {
+    return run_batch(0, nmed, media, nitem, item_med, ks, out, status, precision);
+}
+
+int msgpu_dk_log_det_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                           double* out, int* status, int precision) {
+    return run_batch(1, nmed, media, nitem, item_med, ks, out, status, precision);
+}
+
+int msgpu_amplitude_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                          double* out, double* amps, int* status, int precision) {
+    msgpu_job* J = msgpu_job_create(2, nmed, media, nitem, item_med, ks, precision);
+    if (!J) return MSGPU_E_ARG;
+    int e = msgpu_job_run(J, nullptr);
+    if (!e) e = msgpu_job_results(J, out, status);
+    if (!e && amps) e = msgpu_job_amplitudes(J, amps);
+    msgpu_job_destroy(J);
+    return e;
+}
+
+}  // extern "C"

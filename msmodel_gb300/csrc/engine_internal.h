@@ -1,0 +1,41 @@
+// engine_internal.h -- structures shared by the engine translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "msgpu.h"
+#include "cplx.cuh"
+
+namespace msg {
+
+struct MedDev {
+    int d, n;
+    const double* pos;
+    msgpu_model model;
+};
+
+struct EngineParams {
+    const MedDev* media;
+    const double* ks;     // 2 * nitem
+    const int* item_med;  // nitem
+    const int* order;     // queue position -> item index
+    int nitem;
+    zc* ws;               // per-CTA slots
+    size_t slot;          // complex elements per matrix slot
+    int* piv;             // per-CTA pivots
+    int piv_stride;
+    double* out;          // 2 * nitem
+    int* status;          // nitem
+    unsigned* counter;
+    int kind;             // 0 ln det / n, 1 dlogf, 2 amplitudes a = M^-1 phi
+    double* amps;         // kind 2: a per item (2 * n_i doubles each) or nullptr
+    const long long* amp_off;  // kind 2: offset (in complex elements) of item i in amps
+};
+
+
+// Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
+// negative MSGPU_E* code on error.
+int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st);
+// kernels launched by the mixed engine for one run
+int mixed_launches();
+
+}  // namespace msg

@@ -1,0 +1,299 @@
+"""CPU oracle for the Foldy-Lax hot path (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
+``--impl reference`` legs of ``bench.py`` import this package, and only as
+the checker or the timed CPU baseline.  The product (``msmodel_gb300``)
+never imports it.
+
+``Oracle`` wraps ``liboracle.so`` (the C restatement, ``msoracle.c``);
+``Reference`` wraps ``_ref/libmsref.so`` (the reference sources compiled
+unmodified) when that was built.  Complex scalars are passed as two doubles.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle as _bo
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+MODELS = {"hardsphere": 0, "softsphere": 1, "resonant": 2, "maximum": 3}
+SHAPES = {"cube": 0, "ball": 1, "lattice": 2, "gaussian": 3}
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+class _Model(C.Structure):
+    _fields_ = [("type", C.c_int), ("np", C.c_int), ("p", C.c_double * 2)]
+
+
+def model_struct(model="maximum", params=()):
+    m = _Model()
+    m.type = MODELS[model] if isinstance(model, str) else int(model)
+    m.np = len(params)
+    for i, v in enumerate(params):
+        m.p[i] = v
+    return m
+
+
+def _c2(z):
+    z = complex(z)
+    return np.array([z.real, z.imag], dtype=np.float64)
+
+
+def _cplx_array(zs):
+    zs = np.ascontiguousarray(np.asarray(zs, dtype=np.complex128))
+    return zs.view(np.float64).reshape(-1).copy()
+
+
+class Oracle:
+    """ctypes view of liboracle.so."""
+
+    def __init__(self, lapack=True):
+        path = _bo.build_oracle()
+        L = C.CDLL(path)
+        self.L = L
+        L.orc_set_lapack.argtypes = [C.c_char_p]
+        L.orc_lapack_config.restype = C.c_char_p
+        L.orc_fill_medium.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, _dp]
+        L.orc_rng_init.argtypes = [np.ctypeslib.ndpointer(dtype=np.uint64), C.c_uint64]
+        L.orc_rng_double.argtypes = [np.ctypeslib.ndpointer(dtype=np.uint64)]
+        L.orc_rng_double.restype = C.c_double
+        for f in ("orc_free_green", "orc_dk_free_green", "orc_free_green_imag"):
+            getattr(L, f).argtypes = [C.c_int, _dp, C.c_double, _dp]
+        L.orc_bessel_k.argtypes = [C.c_int, _dp, _dp]
+        L.orc_hyp0f1.argtypes = [C.c_double, _dp, _dp]
+        L.orc_invf.argtypes = [C.POINTER(_Model), C.c_int, _dp, _dp]
+        L.orc_build_ms_matrix.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, _dp]
+        L.orc_build_dk_ms_matrix.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, _dp]
+        L.orc_lu.argtypes = [C.c_int, _dp, _ip, C.c_int]
+        L.orc_tracelog_lu.argtypes = [C.c_int, _dp, C.c_int, _dp]
+        L.orc_dk_log_det.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, C.c_int, _dp]
+        L.orc_total_cross_section.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), C.c_double, C.c_int]
+        L.orc_total_cross_section.restype = C.c_double
+        L.orc_solve.argtypes = [C.c_int, _dp, _dp, C.c_int]
+        L.orc_tracelog_batch.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), C.c_int, _dp, _dp, _ip,
+                                         C.c_int, C.c_int]
+        L.orc_dlogf_batch.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), C.c_int, _dp, _dp, C.c_int,
+                                      C.c_int]
+        L.orc_kplane_args.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
+        L.orc_kcut_args.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.orc_halton_points.argtypes = [_dp, C.c_int, _dp]
+        L.orc_solve_aberth.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, C.c_int, _dp, C.c_int,
+                                       C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)]
+        L.orc_wavefunction.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, C.c_int, C.c_int, _dp, _dp,
+                                       _dp, C.c_int, C.c_int]
+        self.use_lapack = 0
+        if lapack:
+            ob = _bo.openblas_path()
+            if ob is not None and L.orc_set_lapack(ob.encode()) == 0:
+                self.use_lapack = 1
+
+    def lapack_config(self):
+        return self.L.orc_lapack_config().decode()
+
+    # --- medium -----------------------------------------------------------
+    def fill_medium(self, d, n, seed, shape="ball", ratio=1.0):
+        pos = np.zeros(n * d)
+        self.L.orc_fill_medium(d, n, SHAPES[shape] if isinstance(shape, str) else shape, ratio, seed, pos)
+        return pos
+
+    # --- scalar special functions ----------------------------------------
+    def _c(self, fn, *args):
+        out = np.zeros(2)
+        fn(*args, out)
+        return complex(out[0], out[1])
+
+    def free_green(self, d, k, r=1.0):
+        return self._c(self.L.orc_free_green, d, _c2(k), r)
+
+    def dk_free_green(self, d, k, r=1.0):
+        return self._c(self.L.orc_dk_free_green, d, _c2(k), r)
+
+    def free_green_imag(self, d, k, r=1.0):
+        return self._c(self.L.orc_free_green_imag, d, _c2(k), r)
+
+    def bessel_k(self, twonu, z):
+        return self._c(self.L.orc_bessel_k, twonu, _c2(z))
+
+    def hyp0f1(self, a, z):
+        return self._c(self.L.orc_hyp0f1, a, _c2(z))
+
+    def invf(self, d, k, model="maximum", params=()):
+        m = model_struct(model, params)
+        return self._c(self.L.orc_invf, C.byref(m), d, _c2(k))
+
+    # --- matrices ------------------------------------------------------------
+    def ms_matrix(self, d, n, pos, k, model="maximum", params=(), deriv=False):
+        m = model_struct(model, params)
+        out = np.zeros(2 * n * n)
+        fn = self.L.orc_build_dk_ms_matrix if deriv else self.L.orc_build_ms_matrix
+        fn(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m), _c2(k), out)
+        return out.view(np.complex128).reshape(n, n).T  # column-major -> [row, col]
+
+    def lu(self, a, lapack=None):
+        """LU of the square complex matrix a ([row, col]); returns (lu, ipiv, info)."""
+        n = a.shape[0]
+        buf = np.ascontiguousarray(np.asarray(a, dtype=np.complex128).T).view(np.float64).reshape(-1).copy()
+        ipiv = np.zeros(n, dtype=np.int32)
+        info = self.L.orc_lu(n, buf, ipiv, self.use_lapack if lapack is None else int(lapack))
+        return buf.view(np.complex128).reshape(n, n).T, ipiv, info
+
+    def tracelog_lu(self, a, lapack=None):
+        n = a.shape[0]
+        buf = np.ascontiguousarray(np.asarray(a, dtype=np.complex128).T).view(np.float64).reshape(-1).copy()
+        out = np.zeros(2)
+        self.L.orc_tracelog_lu(n, buf, self.use_lapack if lapack is None else int(lapack), out)
+        return complex(out[0], out[1])
+
+    def dk_log_det(self, d, n, pos, k, model="maximum", params=(), lapack=None):
+        m = model_struct(model, params)
+        out = np.zeros(2)
+        self.L.orc_dk_log_det(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m), _c2(k),
+                              self.use_lapack if lapack is None else int(lapack), out)
+        return complex(out[0], out[1])
+
+    def total_cross_section(self, d, n, pos, k, model="maximum", params=()):
+        m = model_struct(model, params)
+        return self.L.orc_total_cross_section(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m),
+                                              float(k), self.use_lapack)
+
+    def tracelog_batch(self, d, n, pos, ks, model="maximum", params=(), nthreads=None, lapack=None):
+        m = model_struct(model, params)
+        kk = _cplx_array(ks)
+        nk = kk.size // 2
+        out = np.zeros(2 * nk)
+        info = np.zeros(nk, dtype=np.int32)
+        self.L.orc_tracelog_batch(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m), nk, kk, out, info,
+                                  nthreads or os.cpu_count(), self.use_lapack if lapack is None else int(lapack))
+        return out.view(np.complex128).copy(), info
+
+    def dlogf_batch(self, d, n, pos, ks, model="maximum", params=(), nthreads=None, lapack=None):
+        m = model_struct(model, params)
+        kk = _cplx_array(ks)
+        nk = kk.size // 2
+        out = np.zeros(2 * nk)
+        self.L.orc_dlogf_batch(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m), nk, kk, out,
+                               nthreads or os.cpu_count(), self.use_lapack if lapack is None else int(lapack))
+        return out.view(np.complex128).copy()
+
+    # --- grids ---------------------------------------------------------------
+    def kplane_args(self, nx, ny, xmin, xmax, ymin, ymax):
+        out = np.zeros(2 * nx * ny)
+        self.L.orc_kplane_args(nx, ny, xmin, xmax, ymin, ymax, out)
+        return out.view(np.complex128).copy()
+
+    def kcut_args(self, ns, zmin, zmax):
+        out = np.zeros(2 * 3 * (ns + 2))
+        self.L.orc_kcut_args(ns, _c2(zmin), _c2(zmax), out)
+        return out.view(np.complex128).copy()
+
+    def halton_points(self, dom, n):
+        out = np.zeros(2 * n)
+        self.L.orc_halton_points(np.asarray(dom, dtype=np.float64), n, out)
+        return out.view(np.complex128).copy()
+
+    # --- root finder / wavefunction -----------------------------------------
+    def solve_aberth(self, d, n, pos, dom, z0, model="maximum", params=(), nexpsup=4, maxit=30, toler=1e-10,
+                     lapack=None):
+        m = model_struct(model, params)
+        z = _cplx_array(z0)
+        ne = C.c_int(0)
+        nr = self.L.orc_solve_aberth(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m),
+                                     np.asarray(dom, dtype=np.float64), z.size // 2, z, nexpsup, maxit, toler,
+                                     self.use_lapack if lapack is None else int(lapack), C.byref(ne))
+        return z.view(np.complex128)[:nr].copy(), ne.value
+
+    def wavefunction(self, d, n, pos, k, nx, ny, dom, model="maximum", params=(), nthreads=None):
+        m = model_struct(model, params)
+        amp = np.zeros(2 * n)
+        psi = np.zeros(2 * nx * ny)
+        self.L.orc_wavefunction(d, n, np.ascontiguousarray(pos, dtype=np.float64), C.byref(m), _c2(k), nx, ny,
+                                np.asarray(dom, dtype=np.float64), amp, psi, nthreads or os.cpu_count(),
+                                self.use_lapack)
+        return amp.view(np.complex128).copy(), psi.view(np.complex128).copy()
+
+
+class Reference:
+    """ctypes view of oracle/_ref/libmsref.so (reference sources, unmodified)."""
+
+    def __init__(self):
+        path = _bo.build_ref()
+        if path is None:
+            raise FileNotFoundError("reference sources not present; oracle/_ref not built")
+        L = C.CDLL(path)
+        self.L = L
+        med = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_ulong]
+        L.ref_fill.argtypes = med + [_dp]
+        L.ref_green.argtypes = [C.c_int, _dp, C.c_double, _dp]
+        L.ref_dk_green.argtypes = [C.c_int, _dp, C.c_double, _dp]
+        L.ref_bessel_k.argtypes = [C.c_int, _dp, _dp]
+        L.ref_tracelog.argtypes = med + [C.c_int, _dp, _dp]
+        L.ref_matrix.argtypes = med + [_dp, C.c_int, _dp]
+        L.ref_dlogf.argtypes = med + [C.c_int, _dp, _dp]
+        L.ref_total_cross_section.argtypes = med + [C.c_double]
+        L.ref_total_cross_section.restype = C.c_double
+        L.ref_aberth.argtypes = med + [_dp, C.c_int, _dp, C.c_int, C.c_int, C.c_double]
+        L.ref_wavefunction.argtypes = med + [_dp, C.c_int, C.c_int, _dp, _dp, _dp]
+
+    @staticmethod
+    def _med(d, n, model, params, shape, ratio, seed):
+        p = np.zeros(2)
+        p[:len(params)] = params
+        return [d, n, MODELS[model], len(params), p, SHAPES[shape], ratio, seed]
+
+    def fill_medium(self, d, n, seed, model="maximum", params=(), shape="ball", ratio=1.0):
+        pos = np.zeros(n * d)
+        self.L.ref_fill(*self._med(d, n, model, params, shape, ratio, seed), pos)
+        return pos
+
+    def free_green(self, d, k, r=1.0):
+        out = np.zeros(2)
+        self.L.ref_green(d, _c2(k), r, out)
+        return complex(*out)
+
+    def dk_free_green(self, d, k, r=1.0):
+        out = np.zeros(2)
+        self.L.ref_dk_green(d, _c2(k), r, out)
+        return complex(*out)
+
+    def bessel_k(self, twonu, z):
+        out = np.zeros(2)
+        self.L.ref_bessel_k(twonu, _c2(z), out)
+        return complex(*out)
+
+    def tracelog(self, d, n, seed, ks, model="maximum", params=(), shape="ball", ratio=1.0):
+        kk = _cplx_array(ks)
+        out = np.zeros_like(kk)
+        self.L.ref_tracelog(*self._med(d, n, model, params, shape, ratio, seed), kk.size // 2, kk, out)
+        return out.view(np.complex128).copy()
+
+    def ms_matrix(self, d, n, seed, k, model="maximum", params=(), deriv=False, shape="ball", ratio=1.0):
+        out = np.zeros(2 * n * n)
+        self.L.ref_matrix(*self._med(d, n, model, params, shape, ratio, seed), _c2(k), int(deriv), out)
+        return out.view(np.complex128).reshape(n, n).T
+
+    def dlogf(self, d, n, seed, ks, model="maximum", params=(), shape="ball", ratio=1.0):
+        kk = _cplx_array(ks)
+        out = np.zeros_like(kk)
+        self.L.ref_dlogf(*self._med(d, n, model, params, shape, ratio, seed), kk.size // 2, kk, out)
+        return out.view(np.complex128).copy()
+
+    def total_cross_section(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
+        return self.L.ref_total_cross_section(*self._med(d, n, model, params, shape, ratio, seed), float(k))
+
+    def solve_aberth(self, d, n, seed, dom, z0, model="maximum", params=(), nexpsup=4, maxit=30, toler=1e-10,
+                     shape="ball", ratio=1.0):
+        z = _cplx_array(z0)
+        nr = self.L.ref_aberth(*self._med(d, n, model, params, shape, ratio, seed), np.asarray(dom, dtype=float),
+                               z.size // 2, z, nexpsup, maxit, toler)
+        return z.view(np.complex128)[:nr].copy()
+
+    def wavefunction(self, d, n, seed, k, nx, ny, dom, model="maximum", params=(), shape="ball", ratio=1.0):
+        amp = np.zeros(2 * n)
+        psi = np.zeros(2 * nx * ny)
+        self.L.ref_wavefunction(*self._med(d, n, model, params, shape, ratio, seed), _c2(k), nx, ny,
+                                np.asarray(dom, dtype=float), amp, psi)
+        return amp.view(np.complex128).copy(), psi.view(np.complex128).copy()

@@ -1,0 +1,78 @@
+"""Build recipe for the CPU oracle (test infrastructure).
+
+* ``oracle/liboracle.so`` -- the C restatement in ``msoracle.c`` (always).
+* ``oracle/_ref/libmsref.so`` -- the reference MSModel sources compiled
+  unmodified from ``/root/reference/src/core`` together with
+  ``ref_driver.c`` and ``lapack_shim.c``; only where the reference tree
+  exists (it is absent on GPU machines, where the oracle alone is used).
+
+Outputs go only to ``oracle/`` and ``oracle/_ref/`` (both git-ignored).
+"""
+import glob
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = "/root/reference"
+# the reference's hot-path translation units (and what they pull in)
+REF_SOURCES = [
+    "ms_matrix_util.c", "green_bessel.c", "medium_util.c", "nru_random.c",
+    "scattering_model_util.c", "real_vector_util.c", "complex_vector_util.c",
+    "common_util.c", "root_finder.c", "domain_util.c",
+]
+
+
+def openblas_path():
+    """Locate the OpenBLAS shipped inside the installed scipy wheel."""
+    import scipy
+    base = os.path.dirname(os.path.dirname(scipy.__file__))
+    cands = sorted(glob.glob(os.path.join(base, "scipy.libs", "libscipy_openblas*.so*")))
+    cands += sorted(glob.glob(os.path.join(os.path.dirname(scipy.__file__), ".libs", "libscipy_openblas*.so*")))
+    return cands[0] if cands else None
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        raise RuntimeError("oracle build failed")
+
+
+def _stale(out, deps):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_oracle(force=False):
+    out = os.path.join(HERE, "liboracle.so")
+    src = [os.path.join(HERE, "msoracle.c"), os.path.join(HERE, "msoracle.h")]
+    if force or _stale(out, src):
+        _run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-o", out, src[0], "-ldl", "-lm"])
+    return out
+
+
+def build_ref(force=False):
+    core = os.path.join(REF_ROOT, "src", "core")
+    if not os.path.isdir(core):
+        return None
+    ob = openblas_path()
+    if ob is None:
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libmsref.so")
+    srcs = [os.path.join(core, s) for s in REF_SOURCES]
+    mine = [os.path.join(HERE, "ref_driver.c"), os.path.join(HERE, "lapack_shim.c")]
+    if force or _stale(out, mine):
+        _run(["gcc", "-O2", "-fms-extensions", "-fopenmp", "-fPIC", "-shared", "-w", "-I", core, "-o", out]
+             + srcs + mine
+             + [ob, "-Wl,-rpath," + os.path.dirname(ob), "-lm"])
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

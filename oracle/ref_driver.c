@@ -1,0 +1,144 @@
+/*
+ * ref_driver.c -- plain-pointer entry points over the reference MSModel
+ * sources (compiled unmodified from src/core into oracle/_ref).  Used only to
+ * pin the oracle restatement (msoracle.c) to the reference itself; test
+ * infrastructure, never part of the product.  Complex values are double[2].
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <complex.h>
+#include "dcomplex_type.h"
+#include "medium_type.h"
+#include "medium_util.h"
+#include "green_bessel.h"
+#include "ms_matrix_util.h"
+#include "root_finder.h"
+#include "scattering_model_util.h"
+
+void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
+
+static void make_medium(Medium* med, int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                        unsigned long seed) {
+    ScatteringModel sm;
+    init_scmodel(&sm, (ScatteringType)mtype, np, (double*)p);
+    init_medium(med, d, n, &sm, (Shape)shape, ratio);
+    del_scmodel(&sm);
+    fill_medium(med, seed);
+}
+static void drop_medium(Medium* med) {
+    del_scmodel(med->scmodel);
+    del_medium(med);
+}
+
+void ref_fill(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+              double* pos) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    memcpy(pos, med.pos, sizeof(double) * (size_t)n * d);
+    drop_medium(&med);
+}
+
+void ref_green(int d, const double* k, double r, double* out) {
+    dcomplex g = free_green(d, k[0] + I * k[1], r);
+    out[0] = creal(g); out[1] = cimag(g);
+}
+void ref_dk_green(int d, const double* k, double r, double* out) {
+    dcomplex g = dk_free_green(d, k[0] + I * k[1], r);
+    out[0] = creal(g); out[1] = cimag(g);
+}
+void ref_bessel_k(int twonu, const double* z, double* out) {
+    dcomplex g = bessel_k(twonu, z[0] + I * z[1]);
+    out[0] = creal(g); out[1] = cimag(g);
+}
+
+/* build_ms_matrix + tracelog_lu for each k (ms_core.c:124-126 loop body) */
+void ref_tracelog(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+                  int nk, const double* ks, double* out) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    dcomplex* a = (dcomplex*)malloc(sizeof(dcomplex) * (size_t)n * n);
+    for (int l = 0; l < nk; l++) {
+        build_ms_matrix(&med, ks[2 * l] + I * ks[2 * l + 1], a);
+        dcomplex t = tracelog_lu(n, a);
+        out[2 * l] = creal(t); out[2 * l + 1] = cimag(t);
+    }
+    free(a);
+    drop_medium(&med);
+}
+
+void ref_matrix(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+                const double* k, int deriv, double* mat) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    if (deriv) build_dk_ms_matrix(&med, k[0] + I * k[1], (dcomplex*)mat);
+    else build_ms_matrix(&med, k[0] + I * k[1], (dcomplex*)mat);
+    drop_medium(&med);
+}
+
+void ref_dlogf(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+               int nk, const double* ks, double* out) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    for (int l = 0; l < nk; l++) {
+        dcomplex t = dk_log_det_ms(&med, ks[2 * l] + I * ks[2 * l + 1]);
+        out[2 * l] = creal(t); out[2 * l + 1] = cimag(t);
+    }
+    drop_medium(&med);
+}
+
+double ref_total_cross_section(int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                               unsigned long seed, double k) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    double cs = total_cross_section(&med, k);
+    drop_medium(&med);
+    return cs;
+}
+
+/* find_eigenstates_serial_1 (ms_core.c:320-328): Aberth on dk_log_det_ms */
+static Medium* g_med;
+static dcomplex g_dlogf(dcomplex k) { return dk_log_det_ms(g_med, k); }
+int ref_aberth(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+               const double* dom, int nz, double* z, int nexpsup, int maxit, double toler) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    Domain dm = {dom[0], dom[1], dom[2], dom[3]};
+    g_med = &med;
+    int nroot = nz;
+    solve_aberth(g_dlogf, &dm, &nroot, (dcomplex*)z, nexpsup, maxit, toler, 0);
+    drop_medium(&med);
+    return nroot;
+}
+
+/* run_wave_function_omp body for one seed (ms_core.c:616-640), plane source */
+void ref_wavefunction(int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                      unsigned long seed, const double* kk, int nx, int ny, const double* dom, double* amp,
+                      double* psi) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    dcomplex k = kk[0] + I * kk[1];
+    dcomplex* a = (dcomplex*)malloc(sizeof(dcomplex) * (size_t)n * n);
+    dcomplex* v = (dcomplex*)amp;
+    int* ipiv = (int*)malloc(sizeof(int) * (size_t)n);
+    int nrhs = 1, info;
+    for (int i = 0; i < n; i++) v[i] = cexp(I * k * med.pos[i * d]);
+    build_ms_matrix(&med, k, a);
+    zgesv_(&n, &nrhs, a, &n, ipiv, v, &n, &info);
+    double dx = (dom[1] - dom[0]) / (nx - 1), dy = (dom[3] - dom[2]) / (ny - 1);
+    double* r = (double*)calloc((size_t)d, sizeof(double));
+    for (int l = 0; l < nx * ny; l++) {
+        r[0] = dom[0] + (l % nx) * dx;
+        r[1] = dom[3] - (l / nx) * dy;
+        dcomplex s = 0.;
+        for (int i = 0; i < n; i++) {
+            double r2 = 0.;
+            for (int c = 0; c < d; c++) { double t = med.pos[i * d + c] - r[c]; r2 += t * t; }
+            s += v[i] * free_green(d, k, sqrt(r2));
+        }
+        s += cexp(I * k * r[0]);
+        psi[2 * l] = creal(s); psi[2 * l + 1] = cimag(s);
+    }
+    free(r); free(a); free(ipiv);
+    drop_medium(&med);
+}

@@ -1,0 +1,52 @@
+/* Calls the symbol-compatible drop-ins exactly as the reference's C callers
+ * do (double _Complex by value, Medium by pointer) and prints the results
+ * for tests/test_gpu_dropin.py to compare with the oracle. */
+#include <complex.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include "msgpu.h"
+#include "msgpu_dropin.h"
+
+static msgpu_dcomplex arg_cut(void* self, int l) {
+    (void)self;
+    /* a kcut of 4 samples from 0.5-0.05i to 3-0.05i (get_arg_ccut order) */
+    int ns = 4, il = l / 3, it = l % 3;
+    msgpu_dcomplex zmin = 0.5 - 0.05 * I, zmax = 3.0 - 0.05 * I, dz = (zmax - zmin) / (ns - 1);
+    return ((ns - il) * zmin + (il - 1) * zmax) / (ns - 1) + I * dz * (it - 1);
+}
+
+int main(int argc, char** argv) {
+    int d = 3, n = argc > 1 ? atoi(argv[1]) : 80;
+    double p[2] = {0.0, 0.0};
+    msgpu_ref_scmodel sm = {0};
+    sm.type = MSGPU_MAXIMUM;
+    sm.np = 0;
+    sm.p = p;
+    msgpu_ref_medium med = {0};
+    med.d = d;
+    med.n = n;
+    med.ntot = n * d;
+    med.shape = MSGPU_BALL;
+    med.ratio = 1.0;
+    med.scmodel = &sm;
+    med.pos = (double*)malloc(sizeof(double) * n * d);
+    msgpu_fill_medium(d, n, MSGPU_BALL, 1.0, 1, med.pos);
+    msgpu_dcomplex* a = (msgpu_dcomplex*)malloc(sizeof(msgpu_dcomplex) * n * n);
+    msgpu_dcomplex k = 1.3 - 0.07 * I;
+    build_ms_matrix(&med, k, a);
+    printf("M01 %.17g %.17g\n", creal(a[1 * n + 0]), cimag(a[1 * n + 0]));
+    msgpu_dcomplex t = tracelog_lu(n, a);
+    printf("tracelog %.17g %.17g\n", creal(t), cimag(t));
+    msgpu_dcomplex g = dk_log_det_ms(&med, k);
+    printf("dlogf %.17g %.17g\n", creal(g), cimag(g));
+    printf("sigma %.17g\n", total_cross_section(&med, 1.3));
+    msgpu_ref_cdata cd = {0};
+    cd.ntot = 3 * (4 + 2);
+    cd.nseed = 2;
+    cd.data = (msgpu_dcomplex*)calloc(cd.ntot, sizeof(msgpu_dcomplex));
+    cd.get_arg = arg_cut;
+    run_tracelog_omp(&med, &cd, 4);
+    for (int l = 0; l < cd.ntot; l++) printf("cut %d %.17g %.17g\n", l, creal(cd.data[l]), cimag(cd.data[l]));
+    free(a); free(med.pos); free(cd.data);
+    return 0;
+}

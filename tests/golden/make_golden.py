@@ -1,0 +1,157 @@
+"""Generate the golden fixtures under tests/golden/ (run in a container that
+has the reference tree; the fixtures are committed so that nothing at test
+time reads the reference).
+
+1. ``reference_tests.json`` -- the known-answer values held by the reference's
+   own tests, read as text:
+   * src/test/test_ms_matrix.c: test_tracelog, test_dk_log_det_ms,
+     test_total_cross_section (Mathematica values, d=2 N=50/20 hardsphere 0.4,
+     seed 1);
+   * src/test/test_green_bessel_data.h: GREEN_DATA, DK_GREEN_DATA,
+     GREEN_IMAG_DATA, BESSEL_K_DATA, HYP0F1_SERIES_DATA (rows
+     [order, Re z, Im z, Re f, Im f], r = 1).
+2. ``reference_runs.json`` -- outputs of the reference itself, compiled from
+   its sources into oracle/_ref, on the hot-path configurations at sizes that
+   finish in seconds (seeded scatterers, ln det / N, dlogf, roots, psi).
+
+Usage:  python tests/golden/make_golden.py
+"""
+import ast
+import hashlib
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = "/root/reference"
+sys.path.insert(0, ROOT)
+
+
+def _c(z):
+    z = complex(z)
+    return [z.real, z.imag]
+
+
+def _cl(zs):
+    return [_c(z) for z in zs]
+
+
+def _array_text(src, name):
+    m = re.search(r"\b" + re.escape(name) + r"\s*\[\]\s*=\s*\{(.*?)\};", src, re.S)
+    return m.group(1)
+
+
+def _c_complex_list(src, name):
+    items = [s.strip() for s in _array_text(src, name).split(",") if s.strip()]
+    return [complex(ast.literal_eval(s.replace("*I", "j"))) for s in items]
+
+
+def _rows5(src, name):
+    m = re.search(r"\b" + re.escape(name) + r"\s*\[\]\[5\]\s*=\s*\{(.*?)\};", src, re.S)
+    nums = re.findall(r"[-+]?(?:\d+\.?\d*|\.\d+)(?:[eE][-+]?\d+)?", m.group(1))
+    vals = [float(x) for x in nums]
+    assert len(vals) % 5 == 0, name
+    return [vals[i:i + 5] for i in range(0, len(vals), 5)]
+
+
+def reference_tests():
+    t = open(os.path.join(REF, "src/test/test_ms_matrix.c")).read()
+    body = lambda fn: t[t.index("void " + fn + "()"):]
+    tr = body("test_tracelog")
+    dk = body("test_dk_log_det_ms")
+    cs = body("test_total_cross_section")
+    out = {
+        "source": "src/test/test_ms_matrix.c, src/test/test_green_bessel_data.h (values computed by the "
+                  "reference author in Wolfram Mathematica)",
+        "medium": {"d": 2, "model": "hardsphere", "params": [0.4], "shape": "ball", "ratio": 1.0, "seed": 1},
+        "tracelog": {"n": 50, "ks": _cl(_c_complex_list(tr, "ks")),
+                     "expected": _cl(_c_complex_list(tr, "logdet_expc")),
+                     "cite": "src/test/test_ms_matrix.c:52-57 (only Re is compared, :69)"},
+        "dk_log_det": {"n": 50, "ks": _cl(_c_complex_list(dk, "ks")),
+                       "expected": _cl(_c_complex_list(dk, "res_expc")),
+                       "cite": "src/test/test_ms_matrix.c:99-103"},
+        "total_cross_section": {"n": 20, "ks": [z.real for z in _c_complex_list(cs, "ks")],
+                                "expected": [z.real for z in _c_complex_list(cs, "cs_expc")],
+                                "cite": "src/test/test_ms_matrix.c:187-188"},
+    }
+    g = open(os.path.join(REF, "src/test/test_green_bessel_data.h")).read()
+    for name in ("GREEN_DATA", "DK_GREEN_DATA", "GREEN_IMAG_DATA", "BESSEL_K_DATA", "HYP0F1_SERIES_DATA"):
+        out[name] = _rows5(g, name)
+    return out
+
+
+def _pos_digest(pos):
+    return hashlib.sha256(np.ascontiguousarray(pos, dtype="<f8").tobytes()).hexdigest()
+
+
+def reference_runs():
+    from oracle import Oracle, Reference
+    r = Reference()
+    o = Oracle()
+    runs = {"lapack": o.lapack_config(), "cases": []}
+
+    def add(kind, **kw):
+        kw["kind"] = kind
+        runs["cases"].append(kw)
+
+    # seeded media of every configuration (digest + head), drawn by the reference's fill_medium
+    for d, n, seed in [(3, 64, 1), (3, 1024, 1), (2, 2048, 1), (3, 4096, 1), (2, 50, 1), (3, 100, 7), (3, 600, 4096)]:
+        pos = r.fill_medium(d, n, seed)
+        add("medium", d=d, n=n, seed=seed, sha256=_pos_digest(pos), head=pos[:6].tolist())
+    # N for the batched realisations: N_r = 100 + floor(501 u), u from init_random(seed 0) in order
+    st = np.zeros(4, dtype=np.uint64)
+    o.L.orc_rng_init(st, 0)
+    add("realisation_sizes", seed=0, sizes=[100 + int(501 * o.L.orc_rng_double(st)) for _ in range(64)])
+
+    # ln det / N: d=3 N=64 kplane subsample, d=3 N=1024 kcut subsample, d=2 N=2048 kplane subsample
+    ks = o.kplane_args(64, 64, 0.5, 3.0, -0.5, 0.0)
+    sel = list(range(0, 4096, 97))
+    add("tracelog", d=3, n=64, seed=1, model="maximum", idx=sel, ks=_cl(ks[sel]),
+        out=_cl(r.tracelog(3, 64, 1, ks[sel])))
+    kc = 0.5 + 2.5 * np.arange(4096) / 4095 - 0.05j
+    sel = [0, 1365, 2730, 4095]
+    add("tracelog", d=3, n=1024, seed=1, model="maximum", idx=sel, ks=_cl(kc[sel]),
+        out=_cl(r.tracelog(3, 1024, 1, kc[sel])))
+    kp = o.kplane_args(256, 256, 0.5, 4.0, -0.3, 0.0)
+    sel = [0, 32768 + 128, 65535]
+    add("tracelog", d=2, n=2048, seed=1, model="maximum", idx=sel, ks=_cl(kp[sel]),
+        out=_cl(r.tracelog(2, 2048, 1, kp[sel])))
+    # small cases with other models and shapes
+    for model, params in (("hardsphere", (0.4,)), ("softsphere", (0.1,)), ("resonant", (10.0, -0.1))):
+        for d in (2, 3):
+            kk = [1.0 - 0.3j, 4.0 - 0.05j, 7.5 - 1.0j]
+            add("tracelog", d=d, n=40, seed=3, model=model, params=list(params), ks=_cl(kk),
+                out=_cl(r.tracelog(d, 40, 3, kk, model, params)))
+    # dlogf = tr(M^-1 dM/dk)
+    kk = [0.7 - 0.2j, 1.9 - 0.05j, 2.8 - 0.6j]
+    add("dlogf", d=3, n=200, seed=5, model="maximum", ks=_cl(kk), out=_cl(r.dlogf(3, 200, 5, kk)))
+    kk = [1.0 - 0.1j, 3.3 - 0.02j]
+    add("dlogf", d=2, n=300, seed=2, model="maximum", ks=_cl(kk), out=_cl(r.dlogf(2, 300, 2, kk)))
+    # Aberth resonance search on dlogf (find_eigenstates_serial_1), 32 Halton seeds
+    dom = [0.5, 3.0, -1.0, 0.0]
+    for n, seed in ((100, 1), (140, 2)):
+        z0 = o.halton_points(dom, 32)
+        roots = r.solve_aberth(3, n, seed, dom, z0, nexpsup=4, maxit=30, toler=1e-10)
+        add("aberth", d=3, n=n, seed=seed, dom=dom, nseed=32, nexpsup=4, maxit=30, toler=1e-10, roots=_cl(roots))
+    # wavefunction: a = M^-1 phi, psi on a small grid of the z=0 plane
+    n = 256
+    rad = (n / (4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
+    dom = [-rad, rad, -rad, rad]
+    amp, psi = r.wavefunction(3, n, 1, 1.5 + 0j, 16, 16, dom)
+    add("wavefunction", d=3, n=n, seed=1, k=[1.5, 0.0], nx=16, ny=16, dom=dom, amp=_cl(amp), psi=_cl(psi))
+    # total cross section (zgesv path)
+    for k in (0.5, 2.0):
+        add("total_cross_section", d=3, n=120, seed=9, k=k, out=r.total_cross_section(3, 120, 9, k))
+    return runs
+
+
+if __name__ == "__main__":
+    with open(os.path.join(HERE, "reference_tests.json"), "w") as f:
+        json.dump(reference_tests(), f)
+    with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
+        json.dump(reference_runs(), f, indent=0)
+    print("wrote", os.listdir(HERE))

@@ -1,0 +1,51 @@
+"""The symbol-compatible drop-ins called from C exactly as the reference's
+callers call them (double _Complex by value, Medium* layout)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from helpers import branch_distance, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def test_dropin_program(ms, oracle, tmp_path):
+    from msmodel_gb300 import build
+    lib = build.build()
+    exe = tmp_path / "dropin_check"
+    r = subprocess.run(["gcc", "-O1", "-std=gnu11", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "dropin_check.c"), "-o", str(exe), lib,
+                        "-Wl,-rpath," + os.path.dirname(lib), "-lm"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    n = 80
+    out = subprocess.run([str(exe), str(n)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    vals = {}
+    cut = {}
+    for line in out.stdout.splitlines():
+        f = line.split()
+        if f[0] == "cut":
+            cut[int(f[1])] = complex(float(f[2]), float(f[3]))
+        elif f[0] == "sigma":
+            vals["sigma"] = float(f[1])
+        else:
+            vals[f[0]] = complex(float(f[1]), float(f[2]))
+    k = 1.3 - 0.07j
+    pos = oracle.fill_medium(3, n, 1)
+    m = oracle.ms_matrix(3, n, pos, k)
+    assert rel(vals["M01"], m[0, 1]) < 1e-15
+    t = oracle.tracelog_lu(m)
+    assert rel(vals["tracelog"].real, t.real) < 1e-11
+    assert branch_distance(vals["tracelog"].imag, t.imag, n) < 1e-9
+    assert rel(vals["dlogf"], oracle.dk_log_det(3, n, pos, k)) < 1e-10
+    assert rel(vals["sigma"], oracle.total_cross_section(3, n, pos, 1.3)) < 1e-10
+    ks = oracle.kcut_args(4, 0.5 - 0.05j, 3.0 - 0.05j)
+    acc = np.zeros(ks.size, dtype=complex)
+    for s in (1, 2):
+        v, _ = oracle.tracelog_batch(3, n, oracle.fill_medium(3, n, s), ks)
+        acc = ((s - 1) * acc + v) / s
+    got = np.array([cut[l] for l in range(ks.size)])
+    assert np.max(rel(got.real, acc.real)) < 1e-11
