@@ -173,6 +173,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--nk", type=int, default=NK, help="cut points per step (default: the full 4096)")
+    ap.add_argument("--natom", type=int, default=N, help="scatterers (default 1024; smaller only for profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -188,7 +189,8 @@ def main():
     torch.cuda.set_device(lr)
     ms.init(lr)
     seed = rank + 1
-    med = ms.Medium(D, N, seed=seed)
+    natom = args.natom
+    med = ms.Medium(D, natom, seed=seed)
     ks = workload_ks()[:args.nk]
     job = ms.Job("tracelog", [med], ks, precision=args.precision)
     stream = torch.cuda.current_stream()
@@ -217,6 +219,7 @@ def main():
             times.append(e0.elapsed_time(e1) * 1e-3)
     barrier()
     launches = ms.launch_count() - l0
+    phase_cycles = ms.engine_stats() if os.environ.get("MSGPU_STATS") else None
     clocks = clk.summary()
     tot = sum(times)
     if ws > 1:
@@ -259,8 +262,8 @@ def main():
         nsteps = min(args.steps, 2)
         t0 = time.perf_counter()
         for _ in range(nsteps):
-            pos = ms.fill_medium(D, N, seed)
-            m2 = ms.Medium(D, N, pos=pos, seed=seed)
+            pos = ms.fill_medium(D, natom, seed)
+            m2 = ms.Medium(D, natom, pos=pos, seed=seed)
             o2, s2 = ms.tracelog_batch([m2], ks, precision=args.precision)
         e_el = time.perf_counter() - t0
         h2d = pos.nbytes + ks.nbytes + 4 * len(ks) * 2 + 40
@@ -280,11 +283,12 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)" if args.precision == "fp64" else
                 "c128 in / bf16-split tensor LU",
                 "data": "synthetic (seeded scatterers drawn by the reference's generator; no dataset)",
-                "config": {"workload": "kcut d=3 N=1024 4096k Im=-0.05", "d": D, "natom": N, "nk": len(ks),
+                "config": {"workload": f"kcut d=3 N={natom} {len(ks)}k Im=-0.05", "d": D, "natom": natom, "nk": len(ks),
                            "model": "maximum", "shape": "ball", "precision": args.precision,
                            "parallelism": f"replicas x{ws} (one realisation per GPU)",
                            "l2": "flushed between steps (256 MB write); per-CTA working set 5 GB > L2"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+                **({"phase_cycles": phase_cycles} if phase_cycles else {}),
                 "precision": args.precision}
         print(json.dumps(line))
     if ws > 1:

@@ -34,6 +34,8 @@ enum { MSGPU_FP64 = 0, MSGPU_MIXED = 1 };
 #define MSGPU_S_OK 0
 #define MSGPU_S_SINGULAR 1  /* an exactly-zero pivot (LAPACK info > 0), ln det = -inf */
 #define MSGPU_S_NONFINITE 2 /* NaN or Inf reached the result */
+#define MSGPU_S_RANGE 4     /* mixed precision: an entry beyond the FP32-safe range (|M_ij| >= 1e18), no result */
+#define MSGPU_S_TIMEOUT 8   /* a bounded device wait gave up; the result is void */
 
 /* error codes */
 #define MSGPU_E_ARG (-1)
@@ -66,6 +68,12 @@ int msgpu_sm_count(void);
 uint64_t msgpu_launch_count(void);
 /* measured FP64 FMA throughput of the device in TFLOP/s (roofline denominator of the FP64 path) */
 int msgpu_probe_fp64(double* tflops);
+
+/* Tensor-core self-check: one 128 x 64 x 32 bf16 product D = A B^T (A 128x32,
+ * B 64x32, row-major f32 holding small integers) through the engine's tcgen05
+ * operand descriptors; mode bit 0 exchanges the descriptor's two core-matrix
+ * strides, bit 1 negates B.  Used by the tests to pin the operand layout. */
+int msgpu_probe_umma(int mode, const float* A, const float* B, float* D);
 
 /* ---- host-side inputs (bit-exact with the reference) -------------------- */
 /* fill_medium (src/core/medium_util.c:164): seeded scatterers, pos[n*d] */
@@ -129,6 +137,10 @@ int msgpu_job_launches(const msgpu_job* job);
 /* algorithmic real flops of one msgpu_job_run (8/3 n^3 per ln det; 8/3 n^3 + 8 n^3 per dlogf) */
 double msgpu_job_flops(const msgpu_job* job);
 void msgpu_job_destroy(msgpu_job* job);
+/* Per-phase SM cycles, summed over CTAs, of the last mixed-precision run made
+ * with the environment variable MSGPU_STATS set: out[0..6] = assembly, panel,
+ * TRSM, slicing, tensor tiles, solves, items.  Returns the count written. */
+int msgpu_engine_stats(double* out, int n);
 
 #ifdef __cplusplus
 }

@@ -71,6 +71,7 @@ def lib():
     L.msgpu_job_flops.argtypes = [C.c_void_p]
     L.msgpu_job_flops.restype = C.c_double
     L.msgpu_job_destroy.argtypes = [C.c_void_p]
+    L.msgpu_engine_stats.argtypes = [_dp, C.c_int]
     _lib = L
     return L
 
@@ -94,6 +95,17 @@ def probe_fp64_tflops():
     v = C.c_double(0.0)
     _check(lib().msgpu_probe_fp64(C.byref(v)), "probe_fp64")
     return v.value
+
+
+def engine_stats():
+    """Per-phase SM cycles of the last mixed-precision run made with the
+    environment variable MSGPU_STATS set (None otherwise)."""
+    out = np.zeros(8)
+    n = lib().msgpu_engine_stats(out, 8)
+    if n <= 0:
+        return None
+    names = ["assemble", "panel", "trsm", "slice", "tiles", "solve", "items"]
+    return {k: float(v) for k, v in zip(names, out[:n])}
 
 
 def sm_count():

@@ -514,6 +514,8 @@ int msgpu_job_run(msgpu_job* J, void* stream) {
 }
 
 int msgpu_job_launches(const msgpu_job* J) { return J ? 1 : 0; }
+
+int msgpu_engine_stats(double* out, int n) { return mixed_stats(out, n); }
 double msgpu_job_flops(const msgpu_job* J) { return J ? J->flops : 0.0; }
 
 int msgpu_job_results(msgpu_job* J, double* out, int* status) {

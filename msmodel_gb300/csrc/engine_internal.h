@@ -37,5 +37,8 @@ struct EngineParams {
 int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st);
 // kernels launched by the mixed engine for one run
 int mixed_launches();
+// per-phase SM cycles of the last mixed run made with MSGPU_STATS set:
+// assemble, panel, trsm, slice, tiles, solve, items
+int mixed_stats(double* out, int n);
 
 }  // namespace msg

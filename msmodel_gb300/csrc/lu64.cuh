@@ -39,7 +39,8 @@ struct __align__(16) LuSmem {
     int item;
 };
 
-__device__ __forceinline__ void block_argmax(double v, int i, LuSmem& s, int& oi) {
+template <class S>
+__device__ __forceinline__ void block_argmax(double v, int i, S& s, int& oi) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -65,7 +66,8 @@ __device__ __forceinline__ void block_argmax(double v, int i, LuSmem& s, int& oi
 }
 
 // sum of three doubles over the CTA; result valid in every thread
-__device__ __forceinline__ void block_sum3(double& a, double& b, double& c, LuSmem& s) {
+template <class S>
+__device__ __forceinline__ void block_sum3(double& a, double& b, double& c, S& s) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -82,7 +84,7 @@ __device__ __forceinline__ void block_sum3(double& a, double& b, double& c, LuSm
 }
 
 // Factor the panel A[j0:n, j0:j0+jb) in place; interchanges inside the panel only.
-__device__ void panel_factor(zc* __restrict__ A, int n, int j0, int jb, int* __restrict__ ipiv, LuSmem& s) {
+static __device__ void panel_factor(zc* __restrict__ A, int n, int j0, int jb, int* __restrict__ ipiv, LuSmem& s) {
     const int tid = threadIdx.x;
     const int cend = j0 + jb;
     double bv = -1.0;
@@ -193,7 +195,7 @@ __device__ __forceinline__ void col_solve_upper(zc* __restrict__ b, int jb, cons
 
 // Apply the panel's interchanges to every other column and compute
 // U12 = L11^-1 A12 (columns right of the panel).
-__device__ void panel_swaps_trsm(zc* __restrict__ A, int n, int j0, int jb, const int* __restrict__ ipiv,
+static __device__ void panel_swaps_trsm(zc* __restrict__ A, int n, int j0, int jb, const int* __restrict__ ipiv,
                                  LuSmem& s) {
     const int tid = threadIdx.x;
     for (int e = tid; e < NB * NB; e += NT) {
@@ -216,7 +218,7 @@ __device__ void panel_swaps_trsm(zc* __restrict__ A, int n, int j0, int jb, cons
 // C[m x nn] -= Ablk[m x kk] * Bblk[kk x nn] (all column-major); kk <= NB.
 // tri != 0: only tiles that hold some element with row >= col are updated
 // (row/col counted from the C origin plus rofs/cofs).
-__device__ void gemm_sub(zc* __restrict__ C, int ldc, const zc* __restrict__ Ab, int lda, const zc* __restrict__ Bb,
+static __device__ void gemm_sub(zc* __restrict__ C, int ldc, const zc* __restrict__ Ab, int lda, const zc* __restrict__ Bb,
                          int ldb, int m, int nn, int kk, LuSmem& s, int tri = 0, int rofs = 0, int cofs = 0) {
     if (m <= 0 || nn <= 0 || kk <= 0) return;
     const int tid = threadIdx.x;
@@ -276,7 +278,7 @@ __device__ void gemm_sub(zc* __restrict__ C, int ldc, const zc* __restrict__ Ab,
 }
 
 // In-place LU of A (n x n, ld n).  ipiv 0-based.  Sets s.info (1-based first zero pivot).
-__device__ void lu_factor(zc* __restrict__ A, int n, int* __restrict__ ipiv, LuSmem& s) {
+static __device__ void lu_factor(zc* __restrict__ A, int n, int* __restrict__ ipiv, LuSmem& s) {
     for (int j0 = 0; j0 < n; j0 += NB) {
         const int jb = min(NB, n - j0);
         panel_factor(A, n, j0, jb, ipiv, s);
@@ -288,7 +290,7 @@ __device__ void lu_factor(zc* __restrict__ A, int n, int* __restrict__ ipiv, LuS
 }
 
 // ln det(A)/n with the reference's branch: sum log|U_ii| + i (sum Arg U_ii + pi [odd interchanges]).
-__device__ zc lu_tracelog(const zc* __restrict__ A, int n, const int* __restrict__ ipiv, LuSmem& s) {
+static __device__ zc lu_tracelog(const zc* __restrict__ A, int n, const int* __restrict__ ipiv, LuSmem& s) {
     double lr = 0.0, ar = 0.0, odd = 0.0;
     for (int i = threadIdx.x; i < n; i += NT) {
         zc u = A[i + (size_t)i * n];
@@ -304,7 +306,7 @@ __device__ zc lu_tracelog(const zc* __restrict__ A, int n, const int* __restrict
 // tr(A^-1 B) given the LU of A (LAPACK layout) and B (n x n, ld n), B destroyed:
 // B <- P B, forward solve with unit-lower L, backward solve with U restricted
 // to the rows each diagonal element needs (X_jj depends on rows >= j only).
-__device__ zc lu_trace_solve(const zc* __restrict__ A, zc* __restrict__ B, int n, const int* __restrict__ ipiv,
+static __device__ zc lu_trace_solve(const zc* __restrict__ A, zc* __restrict__ B, int n, const int* __restrict__ ipiv,
                              LuSmem& s) {
     const int tid = threadIdx.x;
     for (int col = tid; col < n; col += NT) {
@@ -356,7 +358,7 @@ __device__ zc lu_trace_solve(const zc* __restrict__ A, zc* __restrict__ B, int n
 // interchanges, then blocked forward and backward substitution; each block's
 // small triangle is solved by warp 0 (one row per lane), the rectangular
 // remainder by all threads (one row per thread, coalesced column reads).
-__device__ void lu_solve_vec(const zc* __restrict__ A, zc* __restrict__ x, int n, const int* __restrict__ ipiv,
+static __device__ void lu_solve_vec(const zc* __restrict__ A, zc* __restrict__ x, int n, const int* __restrict__ ipiv,
                              LuSmem& s) {
     const unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, lane = tid & 31;
@@ -422,7 +424,7 @@ __device__ __forceinline__ void pair_elements(int d, zc k, double r, bool want_d
 // Assemble M(k) into A and, if B != nullptr, dM/dk into B (ld n, column-major).
 // Tiles of 32 x 32 pairs above the diagonal are evaluated once and written to
 // both triangles, the mirrored tile through shared memory to keep stores coalesced.
-__device__ void assemble(zc* __restrict__ A, zc* __restrict__ B, int n, int d, const double* __restrict__ pos,
+static __device__ void assemble(zc* __restrict__ A, zc* __restrict__ B, int n, int d, const double* __restrict__ pos,
                          const msgpu_model& mdl, zc k, LuSmem& s) {
     const int tid = threadIdx.x;
     if (tid == 0) {

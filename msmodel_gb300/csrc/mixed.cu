@@ -1,7 +1,865 @@
-// mixed.cu -- mixed-precision engine (placeholder until the tensor-core path lands).
+// mixed.cu -- mixed-precision engine: the LU trailing updates run on the
+// tcgen05 tensor cores as exact products of bf16 slices, everything else in
+// double-float (FP32 hi + lo) on the FP32 pipe, assembly and ln in FP64.
+//
+// Trailing update C -= A B (A: m x K panel, B: K x nn rows, K <= 32, complex):
+//  * every row of A (column of B) is scaled by a power of two so its largest
+//    |Re|, |Im| lies in [1/2, 1), then cut into four integer slices
+//    x 2^(8-e) = s0 + s1 2^-9 + s2 2^-18 + s3 2^-27 (|s_k| <= 256); slice k is
+//    stored as the bf16 value s_k 2^-9k, which is exact (35 bits in all);
+//  * level l = i + j of a slice pair (i, j) is accumulated in its own TMEM
+//    accumulator for l = 0 and l = 1 and in a shared one for l = 2, 3: levels
+//    0 and 1 are sums of integers (in units of 2^-9l) below 2^24 and hence
+//    exact whatever order and rounding the tensor core's FP32 adder uses;
+//    the rest carries ~2^-40 of the leading term.  A numerical study of the
+//    Foldy-Lax matrices (d = 3, N <= 1024, Im k >= -1; d = 2 with moderate
+//    Im k) put ln det within ~3e-9 of FP64 with 4 slices; entries spanning
+//    more than ~1e5 within a row (d = 2 far below the real axis) lose
+//    accuracy (about 1e-7), since the scale is per row;
+//  * complex = 4 real products, Re uses the negate-B bit of the instruction
+//    descriptor: 40 tcgen05.mma (128 x 32 x 16) per K-step into six TMEM
+//    accumulators (3 levels x Re/Im, 192 columns);
+//  * epilogue: C (double-float, global) -= 2^(ea+eb-16) (L0 + L1 + L23).
+// Operand slices are written to global images in the tensor core's
+// core-matrix layout and moved to shared memory by bulk copies (TMA engine).
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cstdlib>
+#include <mutex>
 #include "engine_internal.h"
+#include "lu64.cuh"
+#include "df.cuh"
+#include "umma.cuh"
 
 namespace msg {
-int mixed_run(const EngineParams&, int, int, cudaStream_t) { return MSGPU_E_ARG; }
-int mixed_launches() { return 0; }
+
+constexpr int MT_M = 128;               // tile rows = TMEM lanes
+constexpr int MT_N = 32;                // tile columns
+constexpr int A_SUB = MT_M * NB * 2;    // one 128 x 32 bf16 operand tile: 8 KB
+constexpr int B_SUB = MT_N * NB * 2;    // one 32 x 32 bf16 operand tile: 2 KB
+constexpr int A_BAND = 8 * A_SUB;       // 4 slices x {Re, Im}: 64 KB
+constexpr int B_BAND = 8 * B_SUB;       // 16 KB
+constexpr int TMEM_COLS = 256;          // 6 accumulators x 32 columns (allocation rounded to 2^k)
+constexpr float RANGE_LIMIT = 1.0e18f;  // larger entries leave the safe FP32 exponent range
+
+// per-phase cycle accounting (thread 0, only when X.stats is set)
+enum { PH_ASSEMBLE = 0, PH_PANEL, PH_TRSM, PH_SLICE, PH_TILES, PH_SOLVE, PH_ITEMS, PH_N };
+
+struct MixPanel {
+    float4 T[NB][NB + 1];
+    float4 T2[NB][NB + 1];
+    float4 urow[NB];
+};
+struct MixGemm {
+    uint8_t A[A_BAND];
+    uint8_t B[B_BAND];
+};
+struct MixSmem {
+    union {
+        MixGemm g;
+        MixPanel p;
+    } u;
+    int ea[MT_M];
+    int eb[MT_N];
+    uint64_t bar_a, bar_b, bar_mma;
+    uint32_t tmem;
+    int err;
+    zc diag[2];
+    double red_v[NT / 32];
+    int red_i[NT / 32];
+    double red_s[3][NT / 32];
+    int info, bcast_i, item;
+    unsigned long long stat[PH_N];
+    long long t0;
+};
+
+__device__ __forceinline__ void stat_start(MixSmem& s) {
+    if (threadIdx.x == 0) s.t0 = clock64();
+}
+__device__ __forceinline__ void stat_add(MixSmem& s, int ph) {
+    if (threadIdx.x == 0) {
+        long long t = clock64();
+        s.stat[ph] += (unsigned long long)(t - s.t0);
+        s.t0 = t;
+    }
+}
+
+// per-CTA global scratch of the mixed engine
+struct MixScratch {
+    uint8_t* imgA;   // ceil(nmax/128) * A_BAND per CTA
+    uint8_t* imgB;   // ceil(nmax/64) * B_BAND per CTA
+    int* ea;         // exponents, padded
+    int* eb;
+    size_t a_stride, b_stride, e_stride;
+    int* err;        // device flag: 1 = an mbarrier wait timed out
+    unsigned long long* stats;  // per-phase SM cycles summed over CTAs, or nullptr
+};
+
+
+struct Phases {
+    uint32_t a, b, mma;
+};
+
+// ---------------------------------------------------------------- slicing
+// four pre-scaled bf16 slices of the double-float x (hi, lo) for row exponent e:
+// x 2^(8-e) = s0 + s1 2^-9 + s2 2^-18 + s3 2^-27 with integers |s_k| <= 256
+// (bf16 holds every integer up to 256 exactly); 35 significant bits
+__device__ __forceinline__ void slice4(float h, float l, int e, float* o) {
+    float xh = ldexpf(h, 8 - e), xl = ldexpf(l, 8 - e);
+    float s0 = rintf(xh);
+    df r = two_sum(__fsub_rn(xh, s0), xl);
+    o[0] = s0;
+    float sc = 1.0f / 512.0f;
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        float rh = __fmul_rn(r.h, 512.0f), rl = __fmul_rn(r.l, 512.0f);
+        float sk = rintf(rh);
+        r = two_sum(__fsub_rn(rh, sk), rl);
+        o[k] = sk * sc;
+        sc *= 1.0f / 512.0f;
+    }
+}
+
+__device__ __forceinline__ int row_exponent(float mx) {
+    int e = 0;
+    if (mx > 0.0f) frexpf(mx, &e);
+    return e;
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// One operand row of K <= 32 complex values (stride `st` in float4) -> the 8
+// sub-tiles (slice k, Re/Im) of a band of R rows, row r; exponent returned.
+template <int R>
+__device__ __forceinline__ int slice_operand_row(const float4* __restrict__ src, size_t st, int K, uint8_t* band, int r) {
+    float mx = 0.0f;
+    for (int kk = 0; kk < K; ++kk) {
+        float4 v = src[kk * st];
+        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.z)));
+    }
+    const int e = row_exponent(mx);
+    constexpr int SUB = R * NB * 2;
+    for (int kb = 0; kb < NB / 8; ++kb) {
+        uint32_t w[8][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float re[2][4], im[2][4];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const int kk = kb * 8 + 2 * q + t;
+                if (kk < K) {
+                    float4 v = src[kk * st];
+                    slice4(v.x, v.y, e, re[t]);
+                    slice4(v.z, v.w, e, im[t]);
+                } else {
+#pragma unroll
+                    for (int s = 0; s < 4; ++s) re[t][s] = im[t][s] = 0.0f;
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                w[2 * s][q] = pack2(re[0][s], re[1][s]);
+                w[2 * s + 1][q] = pack2(im[0][s], im[1][s]);
+            }
+        }
+        const uint32_t off = cm_offset(r, kb * 8, R);
+#pragma unroll
+        for (int sub = 0; sub < 8; ++sub)
+            *reinterpret_cast<uint4*>(band + sub * SUB + off) = make_uint4(w[sub][0], w[sub][1], w[sub][2], w[sub][3]);
+    }
+    return e;
+}
+
+// A operand: rows [0, m) of the m x K panel P (column-major, ld), all bands
+__device__ void slice_panel_rows(const float4* __restrict__ P, int ld, int m, int K, uint8_t* img, int* ea) {
+    const int mp = (m + MT_M - 1) / MT_M * MT_M;
+    for (int i = threadIdx.x; i < mp; i += NT) {
+        uint8_t* band = img + (size_t)(i / MT_M) * A_BAND;
+        const int r = i % MT_M;
+        if (i < m) {
+            ea[i] = slice_operand_row<MT_M>(P + i, (size_t)ld, K, band, r);
+        } else {
+            ea[i] = 0;
+            for (int kb = 0; kb < NB / 8; ++kb)
+                for (int sub = 0; sub < 8; ++sub)
+                    *reinterpret_cast<uint4*>(band + sub * A_SUB + cm_offset(r, kb * 8, MT_M)) = make_uint4(0, 0, 0, 0);
+        }
+    }
+}
+
+// B operand: columns [0, nn) of the K x nn block Bp (column-major, ld)
+__device__ void slice_block_cols(const float4* __restrict__ Bp, int ld, int nn, int K, uint8_t* img, int* eb) {
+    const int np = (nn + MT_N - 1) / MT_N * MT_N;
+    for (int j = threadIdx.x; j < np; j += NT) {
+        uint8_t* band = img + (size_t)(j / MT_N) * B_BAND;
+        const int r = j % MT_N;
+        if (j < nn) {
+            eb[j] = slice_operand_row<MT_N>(Bp + (size_t)j * ld, 1, K, band, r);
+        } else {
+            eb[j] = 0;
+            for (int kb = 0; kb < NB / 8; ++kb)
+                for (int sub = 0; sub < 8; ++sub)
+                    *reinterpret_cast<uint4*>(band + sub * B_SUB + cm_offset(r, kb * 8, MT_N)) = make_uint4(0, 0, 0, 0);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- tensor-core update
+// Accumulators (TMEM columns 32 a .. 32 a + 31), one per slice level so that
+// levels 0 and 1 stay exact whatever the tensor core's FP32 summation order
+// and rounding: a = 0/1 level 0 (Re/Im), 2/3 level 1, 4/5 levels 2 and 3.
+__device__ __forceinline__ void issue_tile_mmas(MixSmem& s, uint32_t tmem) {
+    const uint32_t idp = idesc_bf16(MT_M, MT_N, false, false), idn = idesc_bf16(MT_M, MT_N, false, true);
+    const uint32_t a0 = smem_u32(s.u.g.A), b0 = smem_u32(s.u.g.B);
+    // core-matrix strides: K direction (LBO) R/8*128, row direction (SBO) 128
+    auto dA = [&](int k, int c, int ks) { return sdesc(a0 + (k * 2 + c) * A_SUB + ks * 4096, 2048, 128); };
+    auto dB = [&](int k, int c, int ks) { return sdesc(b0 + (k * 2 + c) * B_SUB + ks * 1024, 512, 128); };
+    // slice pairs (i, j) and their accumulator group
+    constexpr int NP = 10;
+    const int PI[NP] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+    const int PJ[NP] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+    const int PG[NP] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2};
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const bool first_of_group = (p == 0 || PG[p - 1] != PG[p]);
+            const uint32_t acc = (ks > 0 || !first_of_group) ? 1u : 0u;
+            const uint32_t tre = tmem + 64 * PG[p], tim = tre + 32;
+            umma_bf16(tre, dA(PI[p], 0, ks), dB(PJ[p], 0, ks), idp, acc);
+            umma_bf16(tre, dA(PI[p], 1, ks), dB(PJ[p], 1, ks), idn, 1);
+            umma_bf16(tim, dA(PI[p], 0, ks), dB(PJ[p], 1, ks), idp, acc);
+            umma_bf16(tim, dA(PI[p], 1, ks), dB(PJ[p], 0, ks), idp, 1);
+        }
+    }
+    umma_commit(&s.bar_mma);
+}
+
+// C[m x nn] -= Ap[m x K] * Bp[K x nn]; all double-float complex, column-major.
+// tri != 0: only tiles holding an element with row >= column are updated.
+// Returns false if a wait timed out (the engine then stops).
+__device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __restrict__ Ap, int lda,
+                               const float4* __restrict__ Bp, int ldb, int m, int nn, int K, int tri, MixSmem& s,
+                               const MixScratch& X, uint32_t tmem, Phases& ph) {
+    if (m <= 0 || nn <= 0 || K <= 0) return true;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint8_t* imgA = X.imgA + (size_t)blockIdx.x * X.a_stride;
+    uint8_t* imgB = X.imgB + (size_t)blockIdx.x * X.b_stride;
+    int* gea = X.ea + (size_t)blockIdx.x * X.e_stride;
+    int* geb = X.eb + (size_t)blockIdx.x * X.e_stride;
+    stat_start(s);
+    slice_panel_rows(Ap, lda, m, K, imgA, gea);
+    slice_block_cols(Bp, ldb, nn, K, imgB, geb);
+    fence_proxy_async_all();
+    __syncthreads();
+    stat_add(s, PH_SLICE);
+    const int nbi = (m + MT_M - 1) / MT_M, nbj = (nn + MT_N - 1) / MT_N;
+    // tile list in row-band order, skipping tiles wholly above the diagonal when tri
+    auto tile_ok = [&](int bi, int bj) { return !tri || bi * MT_M + MT_M - 1 >= bj * MT_N; };
+    auto next_tile = [&](int& bi, int& bj) {
+        do {
+            if (++bj >= nbj) { bj = 0; ++bi; }
+        } while (bi < nbi && !tile_ok(bi, bj));
+    };
+    int bi = 0, bj = 0;
+    if (!tile_ok(bi, bj)) next_tile(bi, bj);
+    if (bi >= nbi) return true;
+    if (tid == 0) {
+        mbar_arrive_expect_tx(&s.bar_a, A_BAND);
+        bulk_g2s(s.u.g.A, imgA + (size_t)bi * A_BAND, A_BAND / 2, &s.bar_a);
+        bulk_g2s(s.u.g.A + A_BAND / 2, imgA + (size_t)bi * A_BAND + A_BAND / 2, A_BAND / 2, &s.bar_a);
+        mbar_arrive_expect_tx(&s.bar_b, B_BAND);
+        bulk_g2s(s.u.g.B, imgB + (size_t)bj * B_BAND, B_BAND, &s.bar_b);
+    }
+    bool ok = true;
+    bool new_band = true;
+    while (bi < nbi) {
+        if (tid < MT_M) s.ea[tid] = gea[bi * MT_M + tid];
+        if (tid < MT_N) s.eb[tid] = geb[bj * MT_N + tid];
+        __syncthreads();
+        if (tid == 0) {
+            bool w = true;
+            if (new_band) {
+                w = mbar_wait(&s.bar_a, ph.a);
+                ph.a ^= 1;
+            }
+            w = w && mbar_wait(&s.bar_b, ph.b);
+            ph.b ^= 1;
+            if (!w) s.err = 1;
+            tc_fence_after();
+            issue_tile_mmas(s, tmem);
+        }
+        const bool mw = mbar_wait(&s.bar_mma, ph.mma);
+        ph.mma ^= 1;
+        if (!mw && lane == 0) s.err = 1;
+        int nbi2 = bi, nbj2 = bj;
+        next_tile(nbi2, nbj2);
+        if (tid == 0 && nbi2 < nbi) {  // operands of the next tile: smem is free once the MMAs completed
+            if (nbi2 != bi) {
+                mbar_arrive_expect_tx(&s.bar_a, A_BAND);
+                bulk_g2s(s.u.g.A, imgA + (size_t)nbi2 * A_BAND, A_BAND / 2, &s.bar_a);
+                bulk_g2s(s.u.g.A + A_BAND / 2, imgA + (size_t)nbi2 * A_BAND + A_BAND / 2, A_BAND / 2, &s.bar_a);
+            }
+            mbar_arrive_expect_tx(&s.bar_b, B_BAND);
+            bulk_g2s(s.u.g.B, imgB + (size_t)nbj2 * B_BAND, B_BAND, &s.bar_b);
+        }
+        tc_fence_after();
+        // epilogue: warp w reads TMEM lanes 32(w%4).. (rows), columns 16(w/4)..+15
+        const int q = warp & 3, hcol = warp >> 2;
+        const int rloc = 32 * q + lane, row = bi * MT_M + rloc;
+        const int ea_r = s.ea[rloc];
+#pragma unroll 1
+        for (int cc = 0; cc < 16; cc += 8) {
+            float g[6][8];
+            const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + 16 * hcol + cc;
+#pragma unroll
+            for (int a = 0; a < 6; ++a) tmem_ld8(base + 32 * a, g[a]);
+            tmem_wait_ld();
+            if (row < m) {
+#pragma unroll 2
+                for (int j = 0; j < 8; ++j) {
+                    const int cl = 16 * hcol + cc + j, col = bj * MT_N + cl;
+                    if (col < nn) {
+                        const float sc = ldexpf(1.0f, ea_r + s.eb[cl] - 16);
+                        float4* p = C + row + (size_t)col * ldc;
+                        dfc c = dfc_load(p);
+                        // level 0 + level 1 is exact as a double-float; level 2+3 added with rounding
+                        df vr = df_add(two_sum(g[0][j] * sc, g[2][j] * sc), df{g[4][j] * sc, 0.0f});
+                        df vi = df_add(two_sum(g[1][j] * sc, g[3][j] * sc), df{g[5][j] * sc, 0.0f});
+                        c.re = df_sub(c.re, vr);
+                        c.im = df_sub(c.im, vi);
+                        dfc_store(p, c);
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        new_band = (nbi2 != bi);
+        bi = nbi2;
+        bj = nbj2;
+        if (s.err) {
+            ok = false;
+            break;
+        }
+    }
+    stat_add(s, PH_TILES);
+    return ok;
+}
+
+// ---------------------------------------------------------------- double-float panel, TRSM, solves
+__device__ void df_panel(float4* __restrict__ A, int n, int j0, int jb, int* __restrict__ ipiv, MixSmem& s) {
+    const int tid = threadIdx.x;
+    const int cend = j0 + jb;
+    double bv = -1.0;
+    int bi = n;
+    for (int i = j0 + tid; i < n; i += NT) {
+        double v = dfc_abs1(dfc_load(A + i + (size_t)j0 * n));
+        if (v > bv) { bv = v; bi = i; }
+    }
+    for (int c = j0; c < cend; ++c) {
+        int p;
+        block_argmax(bv, bi, s, p);
+        if (p >= n) p = c;
+        const dfc piv = dfc_load(A + p + (size_t)c * n);
+        const bool nz = !dfc_is_zero(piv);
+        if (tid == 0) {
+            ipiv[c] = p;
+            if (!nz && s.info == 0) s.info = c + 1;
+        }
+        if (nz && p != c && tid < jb) {
+            const size_t col = (size_t)(j0 + tid) * n;
+            float4 t = A[c + col];
+            A[c + col] = A[p + col];
+            A[p + col] = t;
+        }
+        __syncthreads();
+        if (tid < jb && j0 + tid > c) s.u.p.urow[tid] = A[c + (size_t)(j0 + tid) * n];
+        __syncthreads();
+        bv = -1.0;
+        bi = n;
+        if (nz) {
+            // reciprocal of the pivot in FP64, once per column
+            const zc pz = mk(df_to_double(piv.re), df_to_double(piv.im));
+            const zc rz = 1.0 / pz;
+            const dfc r = dfc{df_from_double(rz.re), df_from_double(rz.im)};
+            for (int i = c + 1 + tid; i < n; i += NT) {
+                float4* pc = A + i + (size_t)c * n;
+                const dfc l = dfc_mul(dfc_load(pc), r);
+                dfc_store(pc, l);
+                if (c + 1 < cend) {
+                    float4* q1 = A + i + (size_t)(c + 1) * n;
+                    const dfc a = dfc_fms(dfc_load(q1), l, dfc_load(&s.u.p.urow[c + 1 - j0]));
+                    dfc_store(q1, a);
+                    double v = dfc_abs1(a);
+                    if (v > bv) { bv = v; bi = i; }
+                    for (int cc = c + 2; cc < cend; ++cc) {
+                        float4* q = A + i + (size_t)cc * n;
+                        dfc_store(q, dfc_fms(dfc_load(q), l, dfc_load(&s.u.p.urow[cc - j0])));
+                    }
+                }
+            }
+        } else if (c + 1 < cend) {
+            for (int i = c + 1 + tid; i < n; i += NT) {
+                double v = dfc_abs1(dfc_load(A + i + (size_t)(c + 1) * n));
+                if (v > bv) { bv = v; bi = i; }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void dcol_lower_unit(float4* __restrict__ b, int jb, const float4 (*T)[NB + 1]) {
+    for (int rb = 0; rb < jb; rb += CH) {
+        dfc y[CH];
+#pragma unroll
+        for (int r = 0; r < CH; ++r) y[r] = (rb + r < jb) ? dfc_load(b + rb + r) : dfc{df{0, 0}, df{0, 0}};
+        for (int q = 0; q < rb; ++q) {
+            const dfc xq = dfc_load(b + q);
+#pragma unroll
+            for (int r = 0; r < CH; ++r) y[r] = dfc_fms(y[r], dfc_load(&T[rb + r][q]), xq);
+        }
+#pragma unroll
+        for (int r = 1; r < CH; ++r)
+#pragma unroll
+            for (int q = 0; q < r; ++q) y[r] = dfc_fms(y[r], dfc_load(&T[rb + r][rb + q]), y[q]);
+#pragma unroll
+        for (int r = 0; r < CH; ++r)
+            if (rb + r < jb) dfc_store(b + rb + r, y[r]);
+    }
+}
+
+// upper solve; T's diagonal holds the reciprocals of U_rr
+__device__ __forceinline__ void dcol_upper(float4* __restrict__ b, int jb, const float4 (*T)[NB + 1]) {
+    for (int rb = ((jb - 1) / CH) * CH; rb >= 0; rb -= CH) {
+        dfc y[CH];
+#pragma unroll
+        for (int r = 0; r < CH; ++r) y[r] = (rb + r < jb) ? dfc_load(b + rb + r) : dfc{df{0, 0}, df{0, 0}};
+        for (int q = rb + CH; q < jb; ++q) {
+            const dfc xq = dfc_load(b + q);
+#pragma unroll
+            for (int r = 0; r < CH; ++r) y[r] = dfc_fms(y[r], dfc_load(&T[rb + r][q]), xq);
+        }
+#pragma unroll
+        for (int r = CH - 1; r >= 0; --r) {
+            if (rb + r < jb) {
+                dfc acc = y[r];
+#pragma unroll
+                for (int q = r + 1; q < CH; ++q) acc = dfc_fms(acc, dfc_load(&T[rb + r][rb + q]), y[q]);
+                y[r] = dfc_mul(acc, dfc_load(&T[rb + r][rb + r]));
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < CH; ++r)
+            if (rb + r < jb) dfc_store(b + rb + r, y[r]);
+    }
+}
+
+__device__ void load_lower_block(const float4* A, int n, int j0, int jb, MixSmem& s) {
+    for (int e = threadIdx.x; e < NB * NB; e += NT) {
+        int r = e % NB, q = e / NB;
+        s.u.p.T[r][q] = (r < jb && q < r) ? A[(j0 + r) + (size_t)(j0 + q) * n] : make_float4(0, 0, 0, 0);
+    }
+    __syncthreads();
+}
+
+__device__ void load_upper_block(const float4* A, int n, int j0, int jb, MixSmem& s) {
+    for (int e = threadIdx.x; e < NB * NB; e += NT) {
+        int r = e % NB, q = e / NB;
+        float4 v = make_float4(0, 0, 0, 0);
+        if (r < jb && q < jb && q > r) v = A[(j0 + r) + (size_t)(j0 + q) * n];
+        if (r == q) {
+            if (r < jb) {
+                const dfc u = dfc_load(A + (j0 + r) + (size_t)(j0 + r) * n);
+                const zc ri = 1.0 / mk(df_to_double(u.re), df_to_double(u.im));
+                const df a = df_from_double(ri.re), b = df_from_double(ri.im);
+                v = make_float4(a.h, a.l, b.h, b.l);
+            } else {
+                v = make_float4(1, 0, 0, 0);
+            }
+        }
+        s.u.p.T[r][q] = v;
+    }
+    __syncthreads();
+}
+
+__device__ void df_swaps_trsm(float4* __restrict__ A, int n, int j0, int jb, const int* __restrict__ ipiv, MixSmem& s) {
+    load_lower_block(A, n, j0, jb, s);
+    for (int col = threadIdx.x; col < n; col += NT) {
+        if (col >= j0 && col < j0 + jb) continue;
+        float4* a = A + (size_t)col * n;
+        for (int c = j0; c < j0 + jb; ++c) {
+            int p = ipiv[c];
+            if (p != c) { float4 t = a[c]; a[c] = a[p]; a[p] = t; }
+        }
+        if (col >= j0 + jb) dcol_lower_unit(a + j0, jb, s.u.p.T);
+    }
+    __syncthreads();
+}
+
+__device__ bool lu_mixed(float4* __restrict__ A, int n, int* __restrict__ ipiv, MixSmem& s, const MixScratch& X,
+                         uint32_t tmem, Phases& ph) {
+    for (int j0 = 0; j0 < n; j0 += NB) {
+        const int jb = min(NB, n - j0);
+        stat_start(s);
+        df_panel(A, n, j0, jb, ipiv, s);
+        stat_add(s, PH_PANEL);
+        df_swaps_trsm(A, n, j0, jb, ipiv, s);
+        stat_add(s, PH_TRSM);
+        const int r0 = j0 + jb;
+        if (!mixed_gemm_sub(A + r0 + (size_t)r0 * n, n, A + r0 + (size_t)j0 * n, n, A + j0 + (size_t)r0 * n, n,
+                            n - r0, n - r0, jb, 0, s, X, tmem, ph))
+            return false;
+    }
+    return true;
+}
+
+// tr(A^-1 B) from the mixed LU of A; B (double-float, n x n) is destroyed
+__device__ bool trace_solve_mixed(const float4* __restrict__ A, float4* __restrict__ B, int n,
+                                  const int* __restrict__ ipiv, MixSmem& s, const MixScratch& X, uint32_t tmem,
+                                  Phases& ph, zc& out) {
+    const int tid = threadIdx.x;
+    for (int col = tid; col < n; col += NT) {
+        float4* b = B + (size_t)col * n;
+        for (int i = 0; i < n; ++i) {
+            int p = ipiv[i];
+            if (p != i) { float4 t = b[i]; b[i] = b[p]; b[p] = t; }
+        }
+    }
+    __syncthreads();
+    for (int j0 = 0; j0 < n; j0 += NB) {
+        const int jb = min(NB, n - j0);
+        load_lower_block(A, n, j0, jb, s);
+        for (int col = tid; col < n; col += NT) dcol_lower_unit(B + (size_t)col * n + j0, jb, s.u.p.T);
+        __syncthreads();
+        const int r0 = j0 + jb;
+        if (!mixed_gemm_sub(B + r0, n, A + r0 + (size_t)j0 * n, n, B + j0, n, n - r0, n, jb, 0, s, X, tmem, ph))
+            return false;
+    }
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = nblk - 1; kb >= 0; --kb) {
+        const int j0 = kb * NB, jb = min(NB, n - j0), ncol = j0 + jb;
+        load_upper_block(A, n, j0, jb, s);
+        for (int col = tid; col < ncol; col += NT) dcol_upper(B + (size_t)col * n + j0, jb, s.u.p.T);
+        __syncthreads();
+        if (!mixed_gemm_sub(B, n, A + (size_t)j0 * n, n, B + j0, n, j0, ncol, jb, 1, s, X, tmem, ph)) return false;
+    }
+    double tr = 0.0, ti = 0.0, z = 0.0;
+    for (int i = tid; i < n; i += NT) {
+        dfc v = dfc_load(B + i + (size_t)i * n);
+        tr += df_to_double(v.re);
+        ti += df_to_double(v.im);
+    }
+    block_sum3(tr, ti, z, s);
+    out = mk(tr, ti);
+    return true;
+}
+
+// assembly in FP64, stored double-float; returns the largest |entry| seen
+__device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int n, int d,
+                             const double* __restrict__ pos, const msgpu_model& mdl, zc k, MixSmem& s) {
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s.diag[0] = invf(mdl, d, k);
+        if (B) s.diag[1] = dk_invf(mdl, d, k);
+    }
+    __syncthreads();
+    const zc dg0 = s.diag[0], dg1 = s.diag[1];
+    float mx = 0.0f;
+    auto cvt = [](zc v) {
+        df a = df_from_double(v.re), b = df_from_double(v.im);
+        return make_float4(a.h, a.l, b.h, b.l);
+    };
+    const int nt = (n + 31) / 32;
+    for (int J = 0; J < nt; ++J) {
+        for (int I = 0; I <= J; ++I) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+                const int i = I * 32 + ii, j = J * 32 + jj;
+                if (i < n && j < n && i <= j) {
+                    zc m, dm = mk(0.0);
+                    if (i < j) {
+                        pair_elements(d, k, atom_distance(d, pos, i, j), B != nullptr, m, dm);
+                    } else {
+                        m = dg0;
+                        dm = dg1;
+                    }
+                    const float4 fm = cvt(m);
+                    mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                    A[i + (size_t)j * n] = fm;
+                    s.u.p.T[jj][ii] = fm;
+                    if (B) {
+                        const float4 fd = cvt(dm);
+                        mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                        B[i + (size_t)j * n] = fd;
+                        s.u.p.T2[jj][ii] = fd;
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int jj = tid & 31, ii = (tid >> 5) + 8 * q;
+                const int i = I * 32 + ii, j = J * 32 + jj;
+                if (j < n && i < j) {
+                    A[j + (size_t)i * n] = s.u.p.T[jj][ii];
+                    if (B) B[j + (size_t)i * n] = s.u.p.T2[jj][ii];
+                }
+            }
+            __syncthreads();
+        }
+    }
+    return mx;
+}
+
+// after block_argmax: the CTA-wide maximum (thread 0 folded the warp maxima into red_v)
+__device__ __forceinline__ double block_max_value(MixSmem& s) {
+    double m = s.red_v[0];
+    for (int w = 1; w < NT / 32; ++w) m = fmax(m, s.red_v[w]);
+    return m;
+}
+
+__device__ zc tracelog_df(const float4* __restrict__ A, int n, const int* __restrict__ ipiv, MixSmem& s) {
+    double lr = 0.0, ar = 0.0, odd = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT) {
+        const dfc u = dfc_load(A + i + (size_t)i * n);
+        const double re = df_to_double(u.re), im = df_to_double(u.im);
+        lr += log(hypot(re, im));
+        ar += atan2(im, re);
+        if (ipiv[i] != i) odd += 1.0;
+    }
+    block_sum3(lr, ar, odd, s);
+    if (fmod(odd, 2.0) == 1.0) ar += PI;
+    return mk(lr / n, ar / n);
+}
+
+__global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScratch X) {
+    extern __shared__ uint8_t smem_raw[];
+    MixSmem& s = *reinterpret_cast<MixSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) {
+        tmem_alloc(&s.tmem, TMEM_COLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        mbar_init(&s.bar_a, 1);
+        mbar_init(&s.bar_b, 1);
+        mbar_init(&s.bar_mma, 1);
+        s.err = 0;
+        for (int i = 0; i < PH_N; ++i) s.stat[i] = 0;
+        fence_mbar_init();
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s.tmem;
+    Phases ph{0, 0, 0};
+    float4* A = reinterpret_cast<float4*>(P.ws) + (size_t)blockIdx.x * P.slot * (P.kind == 1 ? 2 : 1);
+    float4* B = (P.kind == 1) ? A + P.slot : nullptr;
+    int* ipiv = P.piv + (size_t)blockIdx.x * P.piv_stride;
+    bool alive = true;
+    while (alive) {
+        if (tid == 0) {
+            s.item = (int)atomicAdd(P.counter, 1u);
+            s.info = 0;
+        }
+        __syncthreads();
+        const int q = s.item;
+        if (q >= P.nitem) break;
+        const int it = P.order[q];
+        const MedDev md = P.media[P.item_med[it]];
+        const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
+        stat_start(s);
+        const float mx = assemble_df(A, B, md.n, md.d, md.pos, md.model, k, s);
+        stat_add(s, PH_ASSEMBLE);
+        int dummy;
+        block_argmax((double)mx, tid, s, dummy);
+        const double mxd = block_max_value(s);
+        __syncthreads();  // red_v is reused by the next reduction
+        zc res = mk(0.0);
+        int st = 0;
+        if (!(mxd < (double)RANGE_LIMIT)) {
+            st |= MSGPU_S_RANGE;
+            res = mk(nan(""), nan(""));
+        } else if (lu_mixed(A, md.n, ipiv, s, X, tmem, ph)) {
+            if (P.kind == 0) {
+                res = tracelog_df(A, md.n, ipiv, s);
+            } else if (!trace_solve_mixed(A, B, md.n, ipiv, s, X, tmem, ph, res)) {
+                alive = false;
+            }
+        } else {
+            alive = false;
+        }
+        if (!alive) {
+            st |= MSGPU_S_TIMEOUT;
+            res = mk(nan(""), nan(""));
+        }
+        if (tid == 0) {
+            s.stat[PH_ITEMS] += 1;
+            P.out[2 * it] = res.re;
+            P.out[2 * it + 1] = res.im;
+            if (s.info) st |= MSGPU_S_SINGULAR;
+            if (!isfinite(res.re) || !isfinite(res.im)) st |= MSGPU_S_NONFINITE;
+            P.status[it] = st;
+        }
+        __syncthreads();
+    }
+    if (s.err && tid == 0) atomicExch(X.err, 1);
+    if (X.stats && tid == 0)
+        for (int i = 0; i < PH_N; ++i) atomicAdd(X.stats + i, s.stat[i]);
+    // a timed-out wait may leave MMAs in flight: give them a bounded chance to land
+    if (s.err && tid == 0) mbar_wait(&s.bar_mma, ph.mma, 1 << 20);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+std::mutex g_mx;
+uint8_t* g_img = nullptr;
+size_t g_img_bytes = 0;
+int* g_err = nullptr;
+unsigned long long* g_stats = nullptr;
+int g_launches_last = 0;
+}  // namespace
+
+static size_t mixed_smem() { return sizeof(MixSmem) + 1024; }
+
+int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_mx);
+    if (P.kind == 2) return MSGPU_E_ARG;  // amplitude solve: FP64 engine only
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_engine_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mixed_smem()) !=
+            cudaSuccess)
+            return MSGPU_E_CUDA;
+        attr = true;
+    }
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_engine_mixed, NT, mixed_smem()) != cudaSuccess || occ < 1)
+        return MSGPU_E_CUDA;
+    MixScratch X;
+    const int nbA = (nmax + MT_M - 1) / MT_M, nbB = (nmax + MT_N - 1) / MT_N;
+    X.a_stride = (size_t)nbA * A_BAND;
+    X.b_stride = (size_t)nbB * B_BAND;
+    X.e_stride = (size_t)nbA * MT_M + MT_N;
+    const size_t need = (size_t)grid * (X.a_stride + X.b_stride) + 2 * sizeof(int) * grid * X.e_stride + 256;
+    if (need > g_img_bytes) {
+        if (g_img) cudaFree(g_img);
+        g_img = nullptr;
+        g_img_bytes = 0;
+        if (cudaMalloc(&g_img, need) != cudaSuccess) return MSGPU_E_CUDA;
+        g_img_bytes = need;
+    }
+    if (!g_err && cudaMalloc(&g_err, sizeof(int)) != cudaSuccess) return MSGPU_E_CUDA;
+    X.imgA = g_img;
+    X.imgB = g_img + (size_t)grid * X.a_stride;
+    X.ea = reinterpret_cast<int*>(X.imgB + (size_t)grid * X.b_stride);
+    X.eb = X.ea + (size_t)grid * X.e_stride;
+    X.err = g_err;
+    X.stats = nullptr;
+    if (getenv("MSGPU_STATS")) {
+        if (!g_stats && cudaMalloc(&g_stats, sizeof(unsigned long long) * PH_N) != cudaSuccess) return MSGPU_E_CUDA;
+        cudaMemsetAsync(g_stats, 0, sizeof(unsigned long long) * PH_N, st);
+        X.stats = g_stats;
+    }
+    if (cudaMemsetAsync(P.counter, 0, sizeof(unsigned), st) != cudaSuccess) return MSGPU_E_CUDA;
+    k_engine_mixed<<<grid, NT, mixed_smem(), st>>>(P, X);
+    g_launches_last = 1;
+    return cudaGetLastError() == cudaSuccess ? 0 : MSGPU_E_CUDA;
+}
+
+int mixed_launches() { return g_launches_last; }
+
+int mixed_stats(double* out, int n) {
+    if (!g_stats) return 0;
+    unsigned long long h[PH_N];
+    if (cudaMemcpy(h, g_stats, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return MSGPU_E_CUDA;
+    for (int i = 0; i < n && i < PH_N; ++i) out[i] = (double)h[i];
+    return PH_N;
+}
+
+// ---------------------------------------------------------------- layout self-check
+__global__ void __launch_bounds__(128, 1) k_probe_umma(const float* A, const float* B, float* D, int mode,
+                                                       int* err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint8_t* As = sm;
+    uint8_t* Bs = sm + 16384;
+    for (int i = tid; i < 65536 / 16; i += 128) reinterpret_cast<int4*>(sm)[i] = make_int4(0, 0, 0, 0);
+    __syncthreads();
+    for (int e = tid; e < 128 * 32; e += 128) {
+        int r = e / 32, k = e % 32;
+        *reinterpret_cast<__nv_bfloat16*>(As + cm_offset(r, k, 128)) = __float2bfloat16_rn(A[e]);
+    }
+    for (int e = tid; e < 64 * 32; e += 128) {
+        int r = e / 32, k = e % 32;
+        *reinterpret_cast<__nv_bfloat16*>(Bs + cm_offset(r, k, 64)) = __float2bfloat16_rn(B[e]);
+    }
+    if (warp == 0) {
+        tmem_alloc(&tbase, 64);
+        tmem_relinquish();
+    }
+    if (tid == 0) mbar_init(&bar, 1);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tbase;
+    if (tid == 0) {
+        uint32_t a0 = smem_u32(As), b0 = smem_u32(Bs);
+        uint32_t lboA = 2048, sboA = 128, lboB = 1024, sboB = 128;
+        if (mode & 1) {
+            lboA = 128; sboA = 2048; lboB = 128; sboB = 1024;
+        }
+        const uint32_t id = idesc_bf16(128, 64, false, (mode & 2) != 0);
+        for (int ks = 0; ks < 2; ++ks)
+            umma_bf16(tmem, sdesc(a0 + ks * 4096, lboA, sboA), sdesc(b0 + ks * 2048, lboB, sboB), id, ks > 0);
+        umma_commit(&bar);
+    }
+    const bool ok = mbar_wait(&bar, 0);
+    if (!ok && lane == 0) atomicExch(err, 1);
+    tc_fence_after();
+    float v[32];
+    for (int half = 0; half < 2; ++half) {
+        tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + half * 32, v);
+        tmem_wait_ld();
+        for (int j = 0; j < 32; ++j) D[(32 * warp + lane) * 64 + half * 32 + j] = v[j];
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
 }  // namespace msg
+
+extern "C" int msgpu_probe_umma(int mode, const float* A, const float* B, float* D) {
+    using namespace msg;
+    if (msgpu_init(-1)) return MSGPU_E_NODEV;
+    float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+    int* derr = nullptr;
+    int herr = 0;
+    if (cudaMalloc(&dA, 128 * 32 * 4) || cudaMalloc(&dB, 64 * 32 * 4) || cudaMalloc(&dD, 128 * 64 * 4) ||
+        cudaMalloc(&derr, 4))
+        return MSGPU_E_CUDA;
+    cudaMemcpy(dA, A, 128 * 32 * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, B, 64 * 32 * 4, cudaMemcpyHostToDevice);
+    cudaMemset(dD, 0, 128 * 64 * 4);
+    cudaMemset(derr, 0, 4);
+    cudaFuncSetAttribute(k_probe_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+    k_probe_umma<<<1, 128, 65536>>>(dA, dB, dD, mode, derr);
+    cudaError_t e = cudaDeviceSynchronize();
+    cudaMemcpy(D, dD, 128 * 64 * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost);
+    cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(derr);
+    if (e != cudaSuccess) return MSGPU_E_CUDA;
+    return herr ? MSGPU_E_CUDA : 0;
+}
