@@ -103,6 +103,7 @@ static __device__ void panel_factor(zc* __restrict__ A, int n, int j0, int jb, i
             ipiv[c] = p;
             if (!nz && s.info == 0) s.info = c + 1;
         }
+        __syncthreads();  // every thread holds the pivot before row p is swapped away
         if (nz && p != c && tid < jb) {
             const size_t col = (size_t)(j0 + tid) * n;
             zc t = A[c + col];

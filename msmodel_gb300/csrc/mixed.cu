@@ -370,6 +370,7 @@ __device__ void df_panel(float4* __restrict__ A, int n, int j0, int jb, int* __r
             ipiv[c] = p;
             if (!nz && s.info == 0) s.info = c + 1;
         }
+        __syncthreads();  // every thread holds the pivot before row p is swapped away
         if (nz && p != c && tid < jb) {
             const size_t col = (size_t)(j0 + tid) * n;
             float4 t = A[c + col];
