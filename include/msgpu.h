@@ -123,6 +123,20 @@ int msgpu_dk_log_det_batch(int nmed, const msgpu_medium* media, int nitem, const
 int msgpu_amplitude_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
                           double* out, double* amps, int* status, int precision);
 
+/* ln det M(k)/n for one medium at nk wave numbers without allocating any
+ * device memory.  For callers that cannot call cudaMalloc (a CUDA graph being
+ * captured, a device whose memory another allocator owns).  No counterpart in
+ * the reference.  All pointers are DEVICE pointers: d_pos[n*d] positions,
+ * d_ks[2*nk] wave numbers, d_out[2*nk] results, d_status[nk] status words;
+ * the work is queued on `stream` (cudaStream_t or NULL) and the call returns
+ * without synchronizing.  Scratch is a fixed 128 MiB __device__ array inside
+ * the library (held by every GPU that loads it): n <= 2048, nk <= 65536, else
+ * MSGPU_E_SIZE.  Calls share that array, so calls that overlap on the GPU
+ * race: keep them on one stream.  The first call on a device looks up the
+ * array's address; make it before any stream capture. */
+int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, msgpu_model model, int nk, const double* d_ks,
+                                 double* d_out, int* d_status, void* stream);
+
 /* Resident jobs: inputs uploaded once, the hot path run on device-resident
  * data (asynchronously on `stream`, a cudaStream_t or NULL), results fetched
  * separately.  kind: 0 = ln det / n, 1 = dlogf, 2 = amplitudes (as above). */
