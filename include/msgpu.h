@@ -137,6 +137,31 @@ int msgpu_amplitude_batch(int nmed, const msgpu_medium* media, int nitem, const 
 int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, msgpu_model model, int nk, const double* d_ks,
                                  double* d_out, int* d_status, void* stream);
 
+/* Resonance search, find_eigenstates_serial_1 (src/core/ms_core.c:320-328) /
+ * solve_aberth (src/core/root_finder.c:522-577) for every medium: the
+ * Maehly-Aberth-Ehrlich iteration on dlogf = tr(M^-1 dM/dk) from the nz
+ * starting points z0 (re, im pairs; the same for every medium), with the
+ * exponential background polynomial of degree nexpsup-1 fitted on 6*nexpsup
+ * Halton samples of dom = {xmin, xmax, ymin, ymax}.  Each sweep evaluates
+ * dlogf for all roots still in progress in one batched GPU job, then replays
+ * the reference's Gauss-Seidel update in FP64.  roots[2*(m*nz + i)] receives
+ * the converged roots of medium m sorted by Re, nroots[m] their number;
+ * *nevals (may be NULL) the dlogf evaluations made. */
+int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, const double* dom, int nz, const double* z0,
+                             int nexpsup, int maxit, double toler, int precision, double* roots, int* nroots,
+                             int* nevals);
+
+/* Wavefunction of run_wave_function_omp (src/core/ms_core.c:596-649), plane
+ * wave along +x: for each medium (realisation, all of equal n and d) the
+ * amplitudes a = M^-1 phi on the GPU, then psi(r) = exp(i k x) + sum_i a_i
+ * G(k,|r - x_i|) on the nx*ny pixel grid of dom = {xmin,xmax,ymin,ymax} in the
+ * (x, y, 0...) plane, row-major from (xmin, ymax) (wave_function_util.c:76).
+ * function/density[nx*ny] receive Re psi and |psi|^2 averaged over the media;
+ * psi (may be NULL) the complex psi of media[0]; amps (may be NULL) a for
+ * every medium (n complex each). */
+int msgpu_wave_function(int nmed, const msgpu_medium* media, const double* k, int nx, int ny, const double* dom,
+                        double* function, double* density, double* psi, double* amps, int precision);
+
 /* Resident jobs: inputs uploaded once, the hot path run on device-resident
  * data (asynchronously on `stream`, a cudaStream_t or NULL), results fetched
  * separately.  kind: 0 = ln det / n, 1 = dlogf, 2 = amplitudes (as above). */

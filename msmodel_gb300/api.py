@@ -72,6 +72,10 @@ def lib():
     L.msgpu_job_flops.restype = C.c_double
     L.msgpu_job_destroy.argtypes = [C.c_void_p]
     L.msgpu_engine_stats.argtypes = [_dp, C.c_int]
+    L.msgpu_wave_function.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, C.c_int, _dp, _dp, _dp, C.c_void_p,
+                                       C.c_void_p, C.c_int]
+    L.msgpu_solve_aberth_batch.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, _dp, C.c_int, C.c_int,
+                                           C.c_double, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -336,6 +340,49 @@ def run_tracelog(d, n, ks, nseed=1, model="maximum", params=(), shape="ball", ra
     for s in range(1, nseed + 1):
         data = ((s - 1) * data + out[(s - 1) * nk:s * nk]) / s
     return data, st
+
+
+def wave_function(media, k, nx, ny, dom, precision="fp64"):
+    """run_wave_function_omp (ms_core.c:596): seed-averaged Re psi and |psi|^2 on
+    the nx x ny grid, plus psi of the first medium and every medium's amplitudes."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    fun = np.zeros(nx * ny)
+    den = np.zeros(nx * ny)
+    psi = np.zeros(2 * nx * ny)
+    amps = np.zeros(2 * sum(m.n for m in media))
+    arr = _media_array(media)
+    _check(lib().msgpu_wave_function(len(media), arr, _c2(k), nx, ny, np.asarray(dom, dtype=np.float64), fun, den,
+                                     psi.ctypes.data, amps.ctypes.data, PRECISION[precision]), "wave_function")
+    a = amps.view(np.complex128)
+    n = media[0].n
+    return fun, den, psi.view(np.complex128).copy(), [a[i * n:(i + 1) * n].copy() for i in range(len(media))]
+
+
+def solve_aberth_batch(media, dom, z0, nexpsup=4, maxit=30, toler=1e-10, precision="fp64"):
+    """solve_aberth on dlogf (root_finder.c:522) for every medium, starting from
+    the same points z0.  Returns (list of root arrays sorted by Re, dlogf evaluations)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    z = _cplx(z0)
+    nz = z.size // 2
+    roots = np.zeros(2 * nz * len(media))
+    nr = np.zeros(len(media), dtype=np.int32)
+    ne = C.c_int(0)
+    arr = _media_array(media)
+    _check(lib().msgpu_solve_aberth_batch(len(media), arr, np.asarray(dom, dtype=np.float64), nz, z, nexpsup,
+                                          maxit, toler, PRECISION[precision], roots, nr, C.byref(ne)),
+           "solve_aberth_batch")
+    rc = roots.view(np.complex128).reshape(len(media), max(nz, 1))
+    return [rc[m, :nr[m]].copy() for m in range(len(media))], ne.value
+
+
+def find_eigenstates(media, dom, ntarget, maxit=30, toler=1e-10, precision="fp64"):
+    """The root search of run_eigenstate_list_serial with method "determinant"
+    (ms_core.c:407-425): ntarget Halton targets sorted by -Im, Aberth with
+    nexpsup = 4, roots finally ordered by -Im (nearest the real axis first)."""
+    z0 = halton_points(dom, ntarget)
+    z0 = z0[np.argsort(-z0.imag, kind="stable")]
+    roots, ne = solve_aberth_batch(media, dom, z0, 4, maxit, toler, precision)
+    return [r[np.argsort(-r.imag, kind="stable")] for r in roots], ne
 
 
 class Job:

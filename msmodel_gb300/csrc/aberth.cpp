@@ -1,0 +1,206 @@
+// aberth.cpp -- batched resonance search: the Maehly-Aberth-Ehrlich iteration
+// of the reference (solve_aberth, src/core/root_finder.c:522-577, driven by
+// find_eigenstates_serial_1, src/core/ms_core.c:320-328) over many
+// realisations at once.
+//
+// In the reference's Gauss-Seidel sweep, root i's dlogf is evaluated at z_i
+// before z_i moves in that sweep, so the dlogf values of all roots still in
+// progress can be computed together at the start of the sweep -- one batched
+// GPU job over every (realisation, root) -- and the sweep then replays the
+// reference's sequential update exactly: the repulsion sum sees the roots
+// j < i already moved.  The updates, flags and the background polynomial
+// (least squares on 6*nexpsup Halton samples, root_finder.c:161) are FP64 on
+// the host; all dlogf evaluations are on the GPU.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+#include "msgpu.h"
+
+namespace {
+
+using cd = std::complex<double>;
+
+bool in_dom(const double* dom, cd z) {  // is_in_domain, src/core/domain_util.c:119 (open bounds)
+    return dom[0] < z.real() && z.real() < dom[1] && dom[2] < z.imag() && z.imag() < dom[3];
+}
+
+// Least squares min |A x - b| for A (m x nc, column-major) by Householder QR;
+// the reference calls zgels_ (root_finder.c:59-68).  x returned in b[0..nc).
+void least_squares(int m, int nc, std::vector<cd>& a, std::vector<cd>& b) {
+    for (int j = 0; j < nc; ++j) {
+        double nrm = 0.0;
+        for (int i = j; i < m; ++i) nrm += std::norm(a[i + j * m]);
+        nrm = std::sqrt(nrm);
+        if (nrm == 0.0) continue;
+        cd x0 = a[j + j * m];
+        cd alpha = (std::abs(x0) > 0 ? -x0 / std::abs(x0) : cd(-1.0)) * nrm;
+        a[j + j * m] -= alpha;
+        double vn = 0.0;
+        for (int i = j; i < m; ++i) vn += std::norm(a[i + j * m]);
+        for (int c = j + 1; c < nc; ++c) {
+            cd s = 0.0;
+            for (int i = j; i < m; ++i) s += std::conj(a[i + j * m]) * a[i + c * m];
+            s = 2.0 * s / vn;
+            for (int i = j; i < m; ++i) a[i + c * m] -= s * a[i + j * m];
+        }
+        cd s = 0.0;
+        for (int i = j; i < m; ++i) s += std::conj(a[i + j * m]) * b[i];
+        s = 2.0 * s / vn;
+        for (int i = j; i < m; ++i) b[i] -= s * a[i + j * m];
+        a[j + j * m] = alpha;
+    }
+    for (int j = nc - 1; j >= 0; --j) {
+        cd s = b[j];
+        for (int c = j + 1; c < nc; ++c) s -= a[j + c * m] * b[c];
+        b[j] = s / a[j + j * m];
+    }
+}
+
+struct Realisation {
+    std::vector<cd> z;
+    std::vector<int> flag;
+    std::vector<cd> poly;
+    int nr = 0;
+    bool aborted = false;
+};
+
+}  // namespace
+
+extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, const double* dom, int nz,
+                                        const double* z0, int nexpsup, int maxit, double toler, int precision,
+                                        double* roots, int* nroots, int* nevals) {
+    if (nmed < 1 || !media || !dom || nz < 0 || (nz > 0 && !z0) || nexpsup < 0 || nexpsup > 16 || maxit < 0 ||
+        !roots || !nroots)
+        return MSGPU_E_ARG;
+    std::vector<Realisation> R(nmed);
+    long long ne = 0;
+    for (int r = 0; r < nmed; ++r) {
+        std::vector<cd>& z = R[r].z;
+        for (int i = 0; i < nz; ++i) z.emplace_back(z0[2 * i], z0[2 * i + 1]);
+        // uniq_cvector (complex_vector_util.c:130): drop near-duplicates, keep order
+        int size = z.empty() ? 0 : 1;
+        for (int i = 1; i < (int)z.size(); ++i) {
+            bool uniq = true;
+            for (int j = 0; j < size; ++j)
+                if (std::abs(z[i] - z[j]) < toler * std::abs(z[i]) || std::abs(z[i] - z[j]) < toler) {
+                    uniq = false;
+                    break;
+                }
+            if (uniq) {
+                std::swap(z[i], z[size]);
+                ++size;
+            }
+        }
+        z.resize(size);
+        // exclude_from_domain (domain_util.c:133), order kept
+        std::vector<cd> kept;
+        for (cd v : z)
+            if (in_dom(dom, v)) kept.push_back(v);
+        z = kept;
+        R[r].nr = (int)z.size();
+        R[r].flag.assign(z.size(), 0);
+        // fewer than two starting points: the reference gives up (root_finder.c:525-528)
+        R[r].aborted = R[r].nr <= 1;
+    }
+    const int deg = nexpsup - 1;
+    if (nexpsup > 0) {
+        const int ns = 6 * nexpsup;
+        std::vector<double> hz(2 * ns);
+        msgpu_halton_points(dom, ns, hz.data());
+        std::vector<int> im;
+        std::vector<double> ks;
+        for (int r = 0; r < nmed; ++r) {
+            if (R[r].aborted) continue;
+            for (int i = 0; i < ns; ++i) {
+                im.push_back(r);
+                ks.push_back(hz[2 * i]);
+                ks.push_back(hz[2 * i + 1]);
+            }
+        }
+        if (!im.empty()) {
+            std::vector<double> out(ks.size());
+            std::vector<int> st(im.size());
+            int e = msgpu_dk_log_det_batch(nmed, media, (int)im.size(), im.data(), ks.data(), out.data(), st.data(),
+                                           precision);
+            if (e) return e;
+            ne += (long long)im.size();
+            size_t q = 0;
+            for (int r = 0; r < nmed; ++r) {
+                if (R[r].aborted) continue;
+                std::vector<cd> a((size_t)ns * nexpsup), b(ns);
+                for (int i = 0; i < ns; ++i, ++q) {
+                    cd zi(hz[2 * i], hz[2 * i + 1]), zp = 1.0;
+                    for (int j = 0; j < nexpsup; ++j) {
+                        a[i + j * ns] = zp;
+                        zp *= zi;
+                    }
+                    b[i] = cd(out[2 * q], out[2 * q + 1]);
+                }
+                least_squares(ns, nexpsup, a, b);
+                R[r].poly.assign(b.begin(), b.begin() + nexpsup);
+            }
+        }
+    }
+    for (int s = 0; s < maxit; ++s) {
+        std::vector<int> im, who;
+        std::vector<double> ks;
+        for (int r = 0; r < nmed; ++r) {
+            if (R[r].aborted) continue;
+            for (int i = 0; i < R[r].nr; ++i)
+                if (R[r].flag[i] == 0) {
+                    im.push_back(r);
+                    who.push_back(i);
+                    ks.push_back(R[r].z[i].real());
+                    ks.push_back(R[r].z[i].imag());
+                }
+        }
+        if (im.empty()) break;
+        std::vector<double> out(ks.size());
+        std::vector<int> st(im.size());
+        int e = msgpu_dk_log_det_batch(nmed, media, (int)im.size(), im.data(), ks.data(), out.data(), st.data(),
+                                       precision);
+        if (e) return e;
+        ne += (long long)im.size();
+        // the sweep in root order, as the reference (root_finder.c:545-565)
+        size_t q = 0;
+        for (int r = 0; r < nmed; ++r) {
+            if (R[r].aborted) continue;
+            Realisation& X = R[r];
+            for (int i = 0; i < X.nr; ++i) {
+                if (X.flag[i] != 0) continue;
+                cd pv = 0.0;
+                if (deg >= 0) {
+                    pv = X.poly[deg];
+                    for (int j = deg - 1; j >= 0; --j) pv = pv * X.z[i] + X.poly[j];
+                }
+                cd inv = cd(out[2 * q], out[2 * q + 1]) - pv;
+                ++q;
+                for (int j = 0; j < X.nr; ++j)
+                    if (j != i) inv -= 1.0 / (X.z[i] - X.z[j]);
+                cd dz = 1.0 / inv, zn = X.z[i] - dz;
+                if (!in_dom(dom, zn)) X.flag[i] = -1;
+                else if (std::abs(dz) < toler * std::abs(X.z[i])) X.flag[i] = 1;
+                else X.z[i] = zn;
+            }
+        }
+    }
+    for (int r = 0; r < nmed; ++r) {
+        Realisation& X = R[r];
+        std::vector<cd> ok;
+        if (X.aborted) {
+            ok = X.z;
+        } else {
+            for (int i = 0; i < X.nr; ++i)
+                if (X.flag[i] == 1) ok.push_back(X.z[i]);
+            std::stable_sort(ok.begin(), ok.end(), [](cd a, cd b) { return a.real() < b.real(); });
+        }
+        nroots[r] = (int)ok.size();
+        for (size_t i = 0; i < ok.size(); ++i) {
+            roots[2 * ((size_t)r * nz + i)] = ok[i].real();
+            roots[2 * ((size_t)r * nz + i) + 1] = ok[i].imag();
+        }
+    }
+    if (nevals) *nevals = (int)std::min<long long>(ne, 2147483647LL);
+    return 0;
+}

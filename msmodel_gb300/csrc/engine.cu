@@ -268,6 +268,14 @@ struct msgpu_job {
 
 extern "C" {
 
+}  // extern "C"
+
+namespace msg {
+void count_launches(int n) { g_launches += n; }
+}  // namespace msg
+
+extern "C" {
+
 int msgpu_init(int device) {
     std::lock_guard<std::mutex> lk(g_mu);
     return init_locked(device);
@@ -503,6 +511,7 @@ int msgpu_job_run(msgpu_job* J, void* stream) {
     P.amps = J->d_amps;
     P.amp_off = J->d_amp_off;
     if (J->precision == MSGPU_MIXED) {
+        if (J->kind == 2) return set_err(MSGPU_E_ARG, "amplitude solve: mixed precision is not available, use MSGPU_FP64");
         int e = mixed_run(P, J->grid, J->nmax, st);
         g_launches += mixed_launches();
         return e;

@@ -32,6 +32,9 @@ struct EngineParams {
 };
 
 
+// adds to the library's count of kernel launches (msgpu_launch_count)
+void count_launches(int n);
+
 // Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
 // negative MSGPU_E* code on error.
 int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st);
