@@ -89,7 +89,9 @@ void msgpu_halton_points(const double* dom, int n, double* z);
 /* which: 0 = G_d(k,r) (free_green, src/core/green_bessel.c:280),
  *        1 = dG/dk (dk_free_green, :311), 2 = I_d(k,r) (free_green_imag, :298),
  *        3 = K_{d/2}(k) (bessel_k with twonu = d, :224; r ignored),
- *        4 = F(k)^-1 of *model (invf, src/core/medium_util.c:296; r ignored) */
+ *        4 = F(k)^-1 of *model (invf, src/core/medium_util.c:296; r ignored),
+ *        5 = the d = 3 element M_ij = -G(k,r) and 6 = dM_ij/dk as the mixed
+ *            engine evaluates them (double-float transcendentals; d ignored) */
 int msgpu_eval_special(int which, int d, const msgpu_model* model, int n, const double* ks, const double* rs,
                        double* out);
 

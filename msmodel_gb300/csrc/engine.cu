@@ -16,6 +16,7 @@
 
 #include "msgpu.h"
 #include "lu64.cuh"
+#include "green_df.cuh"
 #include "engine_internal.h"
 
 using namespace msg;
@@ -156,6 +157,14 @@ __global__ void k_eval_special(int which, int d, msgpu_model m, int n, const dou
     case 1: v = dk_free_green(d, k, r); break;
     case 2: v = free_green_imag(d, k, r); break;
     case 3: v = bessel_k(d, k); break;
+    case 5:
+    case 6: {  // d = 3 matrix elements as the mixed engine evaluates them (double-float)
+        dfc a, b;
+        pair_elements_df3(k, r, which == 6, a, b);
+        const dfc e = which == 5 ? a : b;
+        v = mk(df_to_double(e.re), df_to_double(e.im));
+        break;
+    }
     default: v = invf(m, d, k); break;
     }
     out[2 * i] = v.re;

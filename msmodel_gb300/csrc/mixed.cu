@@ -30,6 +30,7 @@
 #include "lu64.cuh"
 #include "df.cuh"
 #include "umma.cuh"
+#include "green_df.cuh"
 
 namespace msg {
 
@@ -276,10 +277,20 @@ __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __
     }
     bool ok = true;
     bool new_band = true;
+    const int q = warp & 3, hcol = warp >> 2;  // TMEM lane quadrant, column half of this warp
+    const int rloc = 32 * q + lane;
     while (bi < nbi) {
-        if (tid < MT_M) s.ea[tid] = gea[bi * MT_M + tid];
-        if (tid < MT_N) s.eb[tid] = geb[bj * MT_N + tid];
-        __syncthreads();
+        // this thread's row and 16 columns of C, and their exponents, fetched before
+        // the MMAs complete so the memory latency hides behind the tensor core
+        const int row = bi * MT_M + rloc;
+        const bool row_ok = row < m;
+        const int ea_r = row_ok ? gea[row] : 0;
+        float4 cpre[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int col = bj * MT_N + 16 * hcol + j;
+            cpre[j] = (row_ok && col < nn) ? C[row + (size_t)col * ldc] : make_float4(0, 0, 0, 0);
+        }
         if (tid == 0) {
             bool w = true;
             if (new_band) {
@@ -307,31 +318,28 @@ __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __
             bulk_g2s(s.u.g.B, imgB + (size_t)nbj2 * B_BAND, B_BAND, &s.bar_b);
         }
         tc_fence_after();
-        // epilogue: warp w reads TMEM lanes 32(w%4).. (rows), columns 16(w/4)..+15
-        const int q = warp & 3, hcol = warp >> 2;
-        const int rloc = 32 * q + lane, row = bi * MT_M + rloc;
-        const int ea_r = s.ea[rloc];
-#pragma unroll 1
-        for (int cc = 0; cc < 16; cc += 8) {
-            float g[6][8];
+        // epilogue: TMEM lanes 32(w%4).. (rows), columns 16(w/4)..+15
+#pragma unroll
+        for (int cc = 0; cc < 16; cc += 4) {
+            float g[6][4];
             const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + 16 * hcol + cc;
 #pragma unroll
-            for (int a = 0; a < 6; ++a) tmem_ld8(base + 32 * a, g[a]);
+            for (int a = 0; a < 6; ++a) tmem_ld4(base + 32 * a, g[a]);
             tmem_wait_ld();
-            if (row < m) {
-#pragma unroll 2
-                for (int j = 0; j < 8; ++j) {
-                    const int cl = 16 * hcol + cc + j, col = bj * MT_N + cl;
+            if (row_ok) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int col = bj * MT_N + 16 * hcol + cc + j;
                     if (col < nn) {
-                        const float sc = ldexpf(1.0f, ea_r + s.eb[cl] - 16);
-                        float4* p = C + row + (size_t)col * ldc;
-                        dfc c = dfc_load(p);
+                        const float sc = ldexpf(1.0f, ea_r + __ldg(geb + col) - 16);
+                        const float4 cv = cpre[cc + j];
+                        dfc c = dfc{df{cv.x, cv.y}, df{cv.z, cv.w}};
                         // level 0 + level 1 is exact as a double-float; level 2+3 added with rounding
-                        df vr = df_add(two_sum(g[0][j] * sc, g[2][j] * sc), df{g[4][j] * sc, 0.0f});
-                        df vi = df_add(two_sum(g[1][j] * sc, g[3][j] * sc), df{g[5][j] * sc, 0.0f});
+                        const df vr = df_add(two_sum(g[0][j] * sc, g[2][j] * sc), df{g[4][j] * sc, 0.0f});
+                        const df vi = df_add(two_sum(g[1][j] * sc, g[3][j] * sc), df{g[5][j] * sc, 0.0f});
                         c.re = df_sub(c.re, vr);
                         c.im = df_sub(c.im, vi);
-                        dfc_store(p, c);
+                        dfc_store(C + row + (size_t)col * ldc, c);
                     }
                 }
             }
@@ -397,9 +405,20 @@ __device__ void df_panel(float4* __restrict__ A, int n, int j0, int jb, int* __r
                     dfc_store(q1, a);
                     double v = dfc_abs1(a);
                     if (v > bv) { bv = v; bi = i; }
-                    for (int cc = c + 2; cc < cend; ++cc) {
-                        float4* q = A + i + (size_t)cc * n;
-                        dfc_store(q, dfc_fms(dfc_load(q), l, dfc_load(&s.u.p.urow[cc - j0])));
+                    int cc = c + 2;
+                    for (; cc + 4 <= cend; cc += 4) {  // four independent loads in flight
+                        float4 v[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) v[u] = A[i + (size_t)(cc + u) * n];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            dfc_store(A + i + (size_t)(cc + u) * n,
+                                      dfc_fms(dfc{df{v[u].x, v[u].y}, df{v[u].z, v[u].w}}, l,
+                                              dfc_load(&s.u.p.urow[cc + u - j0])));
+                    }
+                    for (; cc < cend; ++cc) {
+                        float4* qp = A + i + (size_t)cc * n;
+                        dfc_store(qp, dfc_fms(dfc_load(qp), l, dfc_load(&s.u.p.urow[cc - j0])));
                     }
                 }
             }
@@ -582,19 +601,28 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                 const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
                 const int i = I * 32 + ii, j = J * 32 + jj;
                 if (i < n && j < n && i <= j) {
-                    zc m, dm = mk(0.0);
-                    if (i < j) {
-                        pair_elements(d, k, atom_distance(d, pos, i, j), B != nullptr, m, dm);
+                    float4 fm, fd = make_float4(0, 0, 0, 0);
+                    if (i < j && d == 3) {
+                        // transcendentals on the FP32 pipe in double-float (green_df.cuh)
+                        dfc a, b;
+                        pair_elements_df3(k, atom_distance(d, pos, i, j), B != nullptr, a, b);
+                        fm = make_float4(a.re.h, a.re.l, a.im.h, a.im.l);
+                        if (B) fd = make_float4(b.re.h, b.re.l, b.im.h, b.im.l);
                     } else {
-                        m = dg0;
-                        dm = dg1;
+                        zc m, dm = mk(0.0);
+                        if (i < j) {
+                            pair_elements(d, k, atom_distance(d, pos, i, j), B != nullptr, m, dm);
+                        } else {
+                            m = dg0;
+                            dm = dg1;
+                        }
+                        fm = cvt(m);
+                        if (B) fd = cvt(dm);
                     }
-                    const float4 fm = cvt(m);
                     mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
                     A[i + (size_t)j * n] = fm;
                     s.u.p.T[jj][ii] = fm;
                     if (B) {
-                        const float4 fd = cvt(dm);
                         mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
                         B[i + (size_t)j * n] = fd;
                         s.u.p.T2[jj][ii] = fd;

@@ -92,3 +92,17 @@ def test_mixed_wide_dynamic_range(ms, oracle):
     got, st = ms.tracelog_batch([med], [2.2 - 0.9j], precision="mixed")
     want, _ = oracle.tracelog_batch(2, 200, med.pos, [2.2 - 0.9j])
     assert st[0] == 0 and rel(got.real, want.real)[0] < 1e-6
+
+
+def test_double_float_elements(ms, oracle):
+    """The mixed engine's d=3 elements (double-float sin/cos/exp on the FP32
+    pipe) agree with the FP64 Green function to 1e-13 relative."""
+    rng = np.random.default_rng(11)
+    ks = rng.uniform(0.05, 6.0, 600) + 1j * rng.uniform(-1.5, 0.2, 600)
+    rs = rng.uniform(0.2, 40.0, 600)
+    m = ms.eval_special(5, 3, ks, rs)
+    dm = ms.eval_special(6, 3, ks, rs)
+    want = -np.array([oracle.free_green(3, k, r) for k, r in zip(ks, rs)])
+    dwant = -np.array([oracle.dk_free_green(3, k, r) for k, r in zip(ks, rs)])
+    assert np.max(rel(m, want)) < 1e-13
+    assert np.max(rel(dm, dwant)) < 1e-13
