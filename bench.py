@@ -130,6 +130,60 @@ def cpu_baseline(seconds=15.0, nk_cap=NK):
                       f"1 OpenBLAS thread ({o.lapack_config().split()[0:2]})", "seconds": el}
 
 
+def measure_mixed(ms, torch, med, ks, out64, args, stream, flush, ws, barrier):
+    """The mixed-precision engine on the same workload in the same process:
+    throughput (resident and end to end), its ratio to the FP64 engine, and
+    the ln det error of every point against the FP64 results."""
+    job = ms.Job("tracelog", [med], ks, precision="mixed")
+    for _ in range(args.warmup):
+        job.run(stream.cuda_stream)
+    barrier()
+    l0 = ms.launch_count()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        job.run(stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    barrier()
+    launches = ms.launch_count() - l0
+    tot = sum(times)
+    if ws > 1:
+        t = torch.tensor([tot], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot = float(t.item())
+    value = args.steps * len(ks) * ws / tot
+    outm, st = job.results()
+    assert np.all(st == 0), "non-zero status in the mixed results"
+    lnd64, lndm = out64 * med.n, outm * med.n
+    relerr = np.abs(lndm.real - lnd64.real) / np.abs(lnd64.real)
+    t0 = time.perf_counter()
+    o2, _ = ms.tracelog_batch([ms.Medium(D, med.n, pos=ms.fill_medium(D, med.n, med.seed), seed=med.seed)], ks,
+                              precision="mixed")
+    e_el = time.perf_counter() - t0
+    n = med.n
+    # bf16 tensor work actually executed: 40 real n x n x 32 slice products per
+    # 32-column panel step (4 real products x 10 slice pairs), i.e. 80/3 n^3 flops
+    tensor_flops = 80.0 / 3.0 * n ** 3 * len(ks) / (tot / args.steps)
+    return {"value": value, "unit": UNIT, "ms_per_step": 1e3 * tot / args.steps, "gpu_launches": launches,
+            "ratio_vs_fp64": None,
+            "e2e": {"value": len(ks) * ws / e_el, "unit": UNIT, "steps": 1},
+            "lndet_rel_err_vs_fp64": {"max": float(relerr.max()), "median": float(np.median(relerr)),
+                                      "points": int(relerr.size)},
+            "im_branch_max_dist": float(np.max(np.abs(((lndm.imag - lnd64.imag) + np.pi) % (2 * np.pi) - np.pi))),
+            "roofline": {"bound": "tensor", "achieved": tensor_flops / 1e12,
+                         "traffic": ((115677166336 + 99175409408) / 304 * len(ks)) if n == N else None,
+                         "peak": read_peaks().get("bf16_tflops_sustained", 1728.6), "unit": "TFLOP/s",
+                         "frac": tensor_flops / 1e12 / read_peaks().get("bf16_tflops_sustained", 1728.6),
+                         "counted": "bf16 tensor flops executed (80/3 n^3 per ln det)",
+                         "algorithmic_tflops": 8.0 / 3.0 * n ** 3 * len(ks) / (tot / args.steps) / 1e12}}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -176,6 +230,7 @@ def main():
     ap.add_argument("--natom", type=int, default=N, help="scatterers (default 1024; smaller only for profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg of an fp64 run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -246,16 +301,12 @@ def main():
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained",
                 "algorithmic": "8/3 N^3 real flops per ln det", "traffic": None}
-    prof = os.path.join(ROOT, "profiles", "engine_traffic.json")
-    if os.path.exists(prof):
-        try:
-            with open(prof) as f:
-                tr = json.load(f).get(args.precision)
-            if tr:
-                roof["traffic"] = tr["bytes_per_eval"] * len(ks)
-                roof["traffic_note"] = tr.get("note")
-        except (OSError, ValueError):
-            pass
+    # DRAM bytes per ln det at N=1024 from one ncu capture of a full wave
+    # (profiles/engine_dram_traffic_kcut_n1024.md), scaled to this launch's points
+    if natom == N:
+        per_eval = {"fp64": (108366984448 + 79019248640) / 304, "mixed": (115677166336 + 99175409408) / 304}
+        roof["traffic"] = per_eval[args.precision] * len(ks)
+        roof["traffic_source"] = "ncu dram__bytes_read+write of a 304-point wave, x points/304"
 
     e2e = None
     if not args.no_e2e:
@@ -273,10 +324,16 @@ def main():
                "api": "msgpu_tracelog_batch (host buffers; includes medium fill, upload, kernels, download)"}
         assert np.max(np.abs(o2 - out)) == 0.0 or np.max(np.abs(o2 - out) / np.abs(out)) < 1e-12
 
+    mixed = None
+    if args.precision == "fp64" and not args.no_mixed:
+        mixed = measure_mixed(ms, torch, med, ks, out, args, stream, flush, ws, barrier)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline()
 
+    if mixed:
+        mixed["ratio_vs_fp64"] = mixed["value"] / value
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
@@ -288,6 +345,7 @@ def main():
                            "parallelism": f"replicas x{ws} (one realisation per GPU)",
                            "l2": "flushed between steps (256 MB write); per-CTA working set 5 GB > L2"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
+                **({"mixed": mixed} if mixed else {}),
                 **({"phase_cycles": phase_cycles} if phase_cycles else {}),
                 "precision": args.precision}
         print(json.dumps(line))
