@@ -27,7 +27,8 @@ namespace msg {
 // right-hand side (kind 2)
 __host__ __device__ inline size_t slot_elems(int kind, size_t slot, int nmax) {
     if (kind == 1) return 2 * slot;
-    if (kind == 2) return slot + (((size_t)nmax + 15) / 16) * 16;
+    // kind 2: the matrix, its copy for the refinement residual (mixed engine), four vectors
+    if (kind == 2) return 2 * slot + 4 * ((((size_t)nmax + 15) / 16) * 16);
     return slot;
 }
 
@@ -250,7 +251,7 @@ int ensure_ws(size_t bytes, void** p) {
 static size_t ws_budget() {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
-    size_t cap = (size_t)48 << 30;
+    size_t cap = (size_t)160 << 30;
     size_t avail = fr + g_ws_bytes;
     return std::min(cap, avail > ((size_t)4 << 30) ? avail - ((size_t)4 << 30) : avail / 2);
 }
@@ -520,7 +521,6 @@ int msgpu_job_run(msgpu_job* J, void* stream) {
     P.amps = J->d_amps;
     P.amp_off = J->d_amp_off;
     if (J->precision == MSGPU_MIXED) {
-        if (J->kind == 2) return set_err(MSGPU_E_ARG, "amplitude solve: mixed precision is not available, use MSGPU_FP64");
         int e = mixed_run(P, J->grid, J->nmax, st);
         g_launches += mixed_launches();
         return e;

@@ -666,6 +666,135 @@ __device__ zc tracelog_df(const float4* __restrict__ A, int n, const int* __rest
     return mk(lr / n, ar / n);
 }
 
+// x <- (LU)^-1 x, one right-hand side, double-float (LAPACK-layout LU): the
+// interchanges, then blocked substitution; each block's triangle by warp 0
+// (one row per lane), the rectangular part by all threads (one row each)
+__device__ void df_solve_vec(const float4* __restrict__ A, float4* __restrict__ x, int n,
+                             const int* __restrict__ ipiv, MixSmem& s) {
+    const unsigned FULL = 0xffffffffu;
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0)
+        for (int i = 0; i < n; ++i) {
+            int p = ipiv[i];
+            if (p != i) { float4 t = x[i]; x[i] = x[p]; x[p] = t; }
+        }
+    __syncthreads();
+    auto shfl4 = [&](float4 v, int src) {
+        return make_float4(__shfl_sync(FULL, v.x, src), __shfl_sync(FULL, v.y, src), __shfl_sync(FULL, v.z, src),
+                           __shfl_sync(FULL, v.w, src));
+    };
+    for (int j0 = 0; j0 < n; j0 += NB) {
+        const int jb = min(NB, n - j0);
+        if (tid < 32) {
+            float4 v = lane < jb ? x[j0 + lane] : make_float4(0, 0, 0, 0);
+            for (int q = 0; q < jb - 1; ++q) {
+                const float4 xq = shfl4(v, q);
+                if (lane > q && lane < jb) {
+                    dfc r = dfc_fms(dfc{df{v.x, v.y}, df{v.z, v.w}}, dfc_load(A + (j0 + lane) + (size_t)(j0 + q) * n),
+                                    dfc{df{xq.x, xq.y}, df{xq.z, xq.w}});
+                    v = make_float4(r.re.h, r.re.l, r.im.h, r.im.l);
+                }
+            }
+            if (lane < jb) x[j0 + lane] = v;
+        }
+        __syncthreads();
+        for (int i = j0 + jb + tid; i < n; i += NT) {
+            dfc acc = dfc_load(x + i);
+            for (int q = 0; q < jb; ++q) acc = dfc_fms(acc, dfc_load(A + i + (size_t)(j0 + q) * n), dfc_load(x + j0 + q));
+            dfc_store(x + i, acc);
+        }
+        __syncthreads();
+    }
+    const int nblk = (n + NB - 1) / NB;
+    for (int kb = nblk - 1; kb >= 0; --kb) {
+        const int j0 = kb * NB, jb = min(NB, n - j0);
+        if (tid < 32) {
+            float4 v = lane < jb ? x[j0 + lane] : make_float4(0, 0, 0, 0);
+            for (int q = jb - 1; q >= 0; --q) {
+                if (lane == q) {
+                    const dfc u = dfc_load(A + (j0 + q) + (size_t)(j0 + q) * n);
+                    const zc xv = mk(df_to_double(df{v.x, v.y}), df_to_double(df{v.z, v.w}));
+                    const zc qv = xv / mk(df_to_double(u.re), df_to_double(u.im));
+                    const df a = df_from_double(qv.re), b = df_from_double(qv.im);
+                    v = make_float4(a.h, a.l, b.h, b.l);
+                }
+                const float4 xq = shfl4(v, q);
+                if (lane < q) {
+                    dfc r = dfc_fms(dfc{df{v.x, v.y}, df{v.z, v.w}}, dfc_load(A + (j0 + lane) + (size_t)(j0 + q) * n),
+                                    dfc{df{xq.x, xq.y}, df{xq.z, xq.w}});
+                    v = make_float4(r.re.h, r.re.l, r.im.h, r.im.l);
+                }
+            }
+            if (lane < jb) x[j0 + lane] = v;
+        }
+        __syncthreads();
+        for (int i = tid; i < j0; i += NT) {
+            dfc acc = dfc_load(x + i);
+            for (int q = 0; q < jb; ++q) acc = dfc_fms(acc, dfc_load(A + i + (size_t)(j0 + q) * n), dfc_load(x + j0 + q));
+            dfc_store(x + i, acc);
+        }
+        __syncthreads();
+    }
+}
+
+// a = M^-1 phi by the mixed LU plus iterative refinement: r = phi - M a with
+// the double-float copy of M, a += (LU)^-1 r in FP64, until |r|/|phi| <= 1e-13
+// (max norms) or 6 corrections.  Returns sigma = -Im(conj(phi).a)/k (the
+// optical theorem of total_cross_section, ms_matrix_util.c:361).
+__device__ zc refine_solve(const float4* __restrict__ LU, const float4* __restrict__ M, const zc* __restrict__ phi,
+                           zc* __restrict__ x, float4* __restrict__ r, float4* __restrict__ t, const MedDev& md,
+                           zc k, const int* __restrict__ ipiv, MixSmem& s) {
+    const int n = md.n, tid = threadIdx.x;
+    auto to4 = [](zc v) {
+        const df a = df_from_double(v.re), b = df_from_double(v.im);
+        return make_float4(a.h, a.l, b.h, b.l);
+    };
+    for (int i = tid; i < n; i += NT) t[i] = to4(phi[i]);
+    __syncthreads();
+    df_solve_vec(LU, t, n, ipiv, s);
+    for (int i = tid; i < n; i += NT) {
+        const dfc v = dfc_load(t + i);
+        x[i] = mk(df_to_double(v.re), df_to_double(v.im));
+    }
+    __syncthreads();
+    double pmax = 0.0;
+    for (int i = tid; i < n; i += NT) pmax = fmax(pmax, zabs(phi[i]));
+    int dummy;
+    block_argmax(pmax, tid, s, dummy);
+    pmax = block_max_value(s);
+    __syncthreads();
+    for (int it = 0; it < 6; ++it) {
+        // r = phi - M x, rows over threads (coalesced columns of M); x as double-floats in t
+        for (int i = tid; i < n; i += NT) t[i] = to4(x[i]);
+        __syncthreads();
+        double rmax = 0.0;
+        for (int i = tid; i < n; i += NT) {
+            dfc acc = dfc{df_from_double(phi[i].re), df_from_double(phi[i].im)};
+            for (int j = 0; j < n; ++j) acc = dfc_fms(acc, dfc_load(M + i + (size_t)j * n), dfc_load(t + j));
+            dfc_store(r + i, acc);
+            rmax = fmax(rmax, fabs(df_to_double(acc.re)) + fabs(df_to_double(acc.im)));
+        }
+        block_argmax(rmax, tid, s, dummy);
+        rmax = block_max_value(s);
+        __syncthreads();
+        if (!(rmax > 1e-13 * pmax)) break;
+        df_solve_vec(LU, r, n, ipiv, s);
+        for (int i = tid; i < n; i += NT) {
+            const dfc v = dfc_load(r + i);
+            x[i] = x[i] + mk(df_to_double(v.re), df_to_double(v.im));
+        }
+        __syncthreads();
+    }
+    double dr = 0.0, di = 0.0, z = 0.0;
+    for (int i = tid; i < n; i += NT) {
+        const zc tt = conjz(phi[i]) * x[i];
+        dr += tt.re;
+        di += tt.im;
+    }
+    block_sum3(dr, di, z, s);
+    return mk(-di, 0.0) / k;
+}
+
 __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScratch X) {
     extern __shared__ uint8_t smem_raw[];
     MixSmem& s = *reinterpret_cast<MixSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -688,8 +817,16 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
     tc_fence_after();
     const uint32_t tmem = s.tmem;
     Phases ph{0, 0, 0};
-    float4* A = reinterpret_cast<float4*>(P.ws) + (size_t)blockIdx.x * P.slot * (P.kind == 1 ? 2 : 1);
+    const size_t vec = (((size_t)P.piv_stride + 15) / 16) * 16;
+    const size_t slot_all = P.kind == 0 ? P.slot : (P.kind == 1 ? 2 * P.slot : 2 * P.slot + 4 * vec);
+    float4* A = reinterpret_cast<float4*>(P.ws) + (size_t)blockIdx.x * slot_all;
     float4* B = (P.kind == 1) ? A + P.slot : nullptr;
+    // kind 2: copy of M, right-hand side phi, solution, residual, correction
+    float4* Mc = A + P.slot;
+    zc* vphi = reinterpret_cast<zc*>(A + 2 * P.slot);
+    zc* vx = vphi + vec;
+    float4* vr = reinterpret_cast<float4*>(vx + vec);
+    float4* vt = vr + vec;
     int* ipiv = P.piv + (size_t)blockIdx.x * P.piv_stride;
     bool alive = true;
     while (alive) {
@@ -715,14 +852,27 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         if (!(mxd < (double)RANGE_LIMIT)) {
             st |= MSGPU_S_RANGE;
             res = mk(nan(""), nan(""));
-        } else if (lu_mixed(A, md.n, ipiv, s, X, tmem, ph)) {
-            if (P.kind == 0) {
-                res = tracelog_df(A, md.n, ipiv, s);
-            } else if (!trace_solve_mixed(A, B, md.n, ipiv, s, X, tmem, ph, res)) {
-                alive = false;
-            }
         } else {
-            alive = false;
+            if (P.kind == 2) {
+                // keep M for the residual; incident plane wave along +x (incident_wave_util.c:76)
+                for (size_t e = tid; e < (size_t)md.n * md.n; e += NT) Mc[e] = A[e];
+                for (int i = tid; i < md.n; i += NT) vphi[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
+                __syncthreads();
+            }
+            if (!lu_mixed(A, md.n, ipiv, s, X, tmem, ph)) {
+                alive = false;
+            } else if (P.kind == 0) {
+                res = tracelog_df(A, md.n, ipiv, s);
+            } else if (P.kind == 1) {
+                if (!trace_solve_mixed(A, B, md.n, ipiv, s, X, tmem, ph, res)) alive = false;
+            } else {
+                res = refine_solve(A, Mc, vphi, vx, vr, vt, md, k, ipiv, s);
+                if (P.amps)
+                    for (int i = tid; i < md.n; i += NT) {
+                        P.amps[2 * (P.amp_off[it] + i)] = vx[i].re;
+                        P.amps[2 * (P.amp_off[it] + i) + 1] = vx[i].im;
+                    }
+            }
         }
         if (!alive) {
             st |= MSGPU_S_TIMEOUT;
@@ -762,7 +912,6 @@ static size_t mixed_smem() { return sizeof(MixSmem) + 1024; }
 
 int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_mx);
-    if (P.kind == 2) return MSGPU_E_ARG;  // amplitude solve: FP64 engine only
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_engine_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mixed_smem()) !=

@@ -106,3 +106,29 @@ def test_double_float_elements(ms, oracle):
     dwant = -np.array([oracle.dk_free_green(3, k, r) for k, r in zip(ks, rs)])
     assert np.max(rel(m, want)) < 1e-13
     assert np.max(rel(dm, dwant)) < 1e-13
+
+
+def test_mixed_amplitudes_refined(ms, oracle):
+    """Mixed LU plus FP64 iterative refinement: the amplitudes a = M^-1 phi reach
+    an FP64 residual |phi - M a| / |phi| <= 1e-12 (checked on the host with the
+    oracle's FP64 matrix) and agree with the FP64 engine to 1e-11 of max|a|."""
+    for d, n, k in [(3, 200, 1.3 + 0j), (3, 333, 2.7 + 0j), (2, 150, 1.1 + 0j)]:
+        med = ms.Medium(d, n, seed=n)
+        sig_m, amps_m, st = ms.amplitude_batch([med], [k], precision="mixed")
+        sig_f, amps_f, _ = ms.amplitude_batch([med], [k], precision="fp64")
+        assert np.all(st == 0)
+        m = oracle.ms_matrix(d, n, med.pos, k)
+        phi = np.exp(1j * k * med.pos[0::d])
+        res = np.max(np.abs(phi - m @ amps_m[0])) / np.max(np.abs(phi))
+        assert res <= 1e-12, res
+        assert np.max(np.abs(amps_m[0] - amps_f[0])) < 1e-11 * np.max(np.abs(amps_f[0]))
+        assert rel(sig_m[0].real, sig_f[0].real) < 1e-11
+
+
+def test_mixed_wavefunction(ms):
+    med = ms.Medium(3, 256, seed=1)
+    rad = (256 / (4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
+    dom = [-rad, rad, -rad, rad]
+    f64 = ms.wave_function([med], 1.5 + 0j, 16, 16, dom, precision="fp64")
+    mix = ms.wave_function([med], 1.5 + 0j, 16, 16, dom, precision="mixed")
+    assert np.max(np.abs(mix[2] - f64[2])) < 1e-11 * np.max(np.abs(f64[2]))
