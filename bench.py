@@ -184,6 +184,71 @@ def measure_mixed(ms, torch, med, ks, out64, args, stream, flush, ws, barrier):
                          "algorithmic_tflops": 8.0 / 3.0 * n ** 3 * len(ks) / (tot / args.steps) / 1e12}}
 
 
+ABERTH_DOM = [0.5, 3.0, -1.0, 0.0]
+
+
+def match_count(got, want, tol):
+    """Roots of `want` that have a distinct root of `got` within tol*|k|."""
+    got = list(np.asarray(got))
+    n = 0
+    for w in np.asarray(want):
+        if not got:
+            break
+        dist = np.abs(np.asarray(got) - w)
+        j = int(np.argmin(dist))
+        if dist[j] <= tol * max(abs(w), 1.0):
+            got.pop(j)
+            n += 1
+    return n
+
+
+def aberth_media(ms, count):
+    """Realisations r = 1..count of the batched resonance search: d=3, N_r drawn
+    from [100, 600] by the reference generator (init_random(0), in order),
+    positions from fill_medium(seed=r)."""
+    sizes = ms.realisation_sizes(count, seed=0)
+    return [ms.Medium(D, n, seed=r + 1) for r, n in enumerate(sizes)]
+
+
+def measure_aberth(ms, torch, count, cpu_sample):
+    """Resonance search (Aberth-Ehrlich on dlogf, 32 Halton seeds, nexpsup 4,
+    maxit 30, toler 1e-10) over `count` realisations: roots/s in FP64 and in
+    mixed precision (FP64 Newton/Aberth update), the agreement of the two root
+    sets, and the reference algorithm on `cpu_sample` realisations on all host
+    cores."""
+    media = aberth_media(ms, count)
+    z0 = ms.halton_points(ABERTH_DOM, 32)
+    res, roots = {}, {}
+    for prec in ("fp64", "mixed"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs, ne = ms.solve_aberth_batch(media, ABERTH_DOM, z0, 4, 30, 1e-10, precision=prec)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        nr = sum(len(r) for r in rs)
+        roots[prec] = rs
+        res[prec] = {"roots_per_s": nr / el, "roots": nr, "dlogf_evals": ne, "dlogf_per_s": ne / el,
+                     "seconds": el}
+    found = sum(match_count(roots["mixed"][i], roots["fp64"][i], 1e-8) for i in range(count))
+    res["mixed_matches_fp64"] = {"matched": found, "fp64_roots": res["fp64"]["roots"],
+                                 "mixed_roots": res["mixed"]["roots"]}
+    if cpu_sample:
+        import concurrent.futures as cf
+        from oracle import Oracle
+        o = Oracle()
+        sample = media[:cpu_sample]
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            outs = list(ex.map(lambda m: o.solve_aberth(D, m.n, m.pos, ABERTH_DOM, z0)[0], sample))
+        el = time.perf_counter() - t0
+        nr = sum(len(r) for r in outs)
+        res["cpu_baseline"] = {"roots_per_s": nr / el, "roots": nr, "realisations": len(sample),
+                               "cores": os.cpu_count(), "kind": "port", "seconds": el}
+    res["config"] = {"realisations": count, "natom": "100..600 (reference generator, seed 0)", "seeds": 32,
+                     "domain": ABERTH_DOM, "nexpsup": 4, "maxit": 30, "toler": 1e-10}
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -231,6 +296,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg of an fp64 run")
+    ap.add_argument("--aberth", type=int, default=32, help="realisations of the resonance-search leg (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -328,6 +394,10 @@ def main():
     if args.precision == "fp64" and not args.no_mixed:
         mixed = measure_mixed(ms, torch, med, ks, out, args, stream, flush, ws, barrier)
 
+    aberth = None
+    if rank == 0 and args.aberth > 0 and args.precision == "fp64":
+        aberth = measure_aberth(ms, torch, args.aberth, 0 if args.no_cpu else min(args.aberth, os.cpu_count() or 1))
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline()
@@ -346,6 +416,7 @@ def main():
                            "l2": "flushed between steps (256 MB write); per-CTA working set 5 GB > L2"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
                 **({"mixed": mixed} if mixed else {}),
+                **({"aberth": aberth} if aberth else {}),
                 **({"phase_cycles": phase_cycles} if phase_cycles else {}),
                 "precision": args.precision}
         print(json.dumps(line))

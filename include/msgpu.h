@@ -78,6 +78,8 @@ int msgpu_probe_umma(int mode, const float* A, const float* B, float* D);
 /* ---- host-side inputs (bit-exact with the reference) -------------------- */
 /* fill_medium (src/core/medium_util.c:164): seeded scatterers, pos[n*d] */
 int msgpu_fill_medium(int d, int n, int shape, double ratio, uint64_t seed, double* pos);
+/* n successive random_double (src/core/nru_random.c:39) after init_random(seed) (:63) */
+void msgpu_random_doubles(uint64_t seed, int n, double* out);
 /* get_arg_cmap (src/core/complex_map_util.c:27) for l = 0..nx*ny-1 */
 void msgpu_kplane_args(int nx, int ny, double xmin, double xmax, double ymin, double ymax, double* ks);
 /* get_arg_ccut (src/core/complex_cut_util.c:32) for l = 0..3(ns+2)-1 */

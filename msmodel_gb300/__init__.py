@@ -8,7 +8,7 @@ from .api import *  # noqa: F401,F403
 from .api import MsgpuError, lib  # noqa: F401
 
 __all__ = [
-    "Medium", "fill_medium", "kplane_args", "kcut_args", "halton_points", "free_green", "dk_free_green",
+    "Medium", "fill_medium", "random_doubles", "realisation_sizes", "kplane_args", "kcut_args", "halton_points", "free_green", "dk_free_green",
     "free_green_imag", "bessel_k", "invf", "build_ms_matrix", "build_dk_ms_matrix", "tracelog_lu",
     "tracelog_batch", "dk_log_det_batch", "amplitude_batch", "dk_log_det_ms", "total_cross_section",
     "run_tracelog", "wave_function", "solve_aberth_batch", "find_eigenstates", "Job", "init", "launch_count", "sm_count", "MsgpuError", "lib",

@@ -51,6 +51,7 @@ def lib():
     L.msgpu_launch_count.restype = C.c_uint64
     L.msgpu_probe_fp64.argtypes = [C.POINTER(C.c_double)]
     L.msgpu_fill_medium.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, _dp]
+    L.msgpu_random_doubles.argtypes = [C.c_uint64, C.c_int, _dp]
     L.msgpu_kplane_args.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
     L.msgpu_kcut_args.argtypes = [C.c_int, _dp, _dp, _dp]
     L.msgpu_halton_points.argtypes = [_dp, C.c_int, _dp]
@@ -176,6 +177,20 @@ def _media_array(media):
     for i, m in enumerate(media):
         arr[i] = m._struct()
     return arr
+
+
+def random_doubles(seed, n):
+    """n values of the reference generator from init_random(seed) (nru_random.c:39, :63)."""
+    out = np.zeros(n)
+    lib().msgpu_random_doubles(seed, n, out)
+    return out
+
+
+def realisation_sizes(count, nmin=100, nmax=600, seed=0):
+    """Sizes of the batched realisations: N_r = nmin + floor((nmax-nmin+1) u_r), u_r drawn
+    in order from init_random(seed)."""
+    u = random_doubles(seed, count)
+    return [nmin + int((nmax - nmin + 1) * x) for x in u]
 
 
 # --------------------------------------------------------------------------- grids

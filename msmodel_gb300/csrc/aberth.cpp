@@ -142,27 +142,26 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
             }
         }
     }
-    for (int s = 0; s < maxit; ++s) {
-        std::vector<int> im, who;
+    // One sweep over every realisation: batched dlogf of the roots in progress,
+    // then the reference's sequential update.  Returns false on a GPU error.
+    auto sweep = [&](int prec, double tol, int& err) -> bool {
+        std::vector<int> im;
         std::vector<double> ks;
         for (int r = 0; r < nmed; ++r) {
             if (R[r].aborted) continue;
             for (int i = 0; i < R[r].nr; ++i)
                 if (R[r].flag[i] == 0) {
                     im.push_back(r);
-                    who.push_back(i);
                     ks.push_back(R[r].z[i].real());
                     ks.push_back(R[r].z[i].imag());
                 }
         }
-        if (im.empty()) break;
+        if (im.empty()) return false;
         std::vector<double> out(ks.size());
         std::vector<int> st(im.size());
-        int e = msgpu_dk_log_det_batch(nmed, media, (int)im.size(), im.data(), ks.data(), out.data(), st.data(),
-                                       precision);
-        if (e) return e;
+        err = msgpu_dk_log_det_batch(nmed, media, (int)im.size(), im.data(), ks.data(), out.data(), st.data(), prec);
+        if (err) return false;
         ne += (long long)im.size();
-        // the sweep in root order, as the reference (root_finder.c:545-565)
         size_t q = 0;
         for (int r = 0; r < nmed; ++r) {
             if (R[r].aborted) continue;
@@ -180,10 +179,33 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
                     if (j != i) inv -= 1.0 / (X.z[i] - X.z[j]);
                 cd dz = 1.0 / inv, zn = X.z[i] - dz;
                 if (!in_dom(dom, zn)) X.flag[i] = -1;
-                else if (std::abs(dz) < toler * std::abs(X.z[i])) X.flag[i] = 1;
+                else if (std::abs(dz) < tol * std::abs(X.z[i])) X.flag[i] = 1;
                 else X.z[i] = zn;
             }
         }
+        return true;
+    };
+    int err = 0;
+    if (precision == MSGPU_MIXED) {
+        // Mixed-precision dlogf loses accuracy as 1/distance to a root (M is
+        // nearly singular there): iterate in mixed precision to a relative step
+        // of 1e-7, then finish every such root with FP64 dlogf and the
+        // reference's tolerance (the Newton/Aberth update itself is FP64 all along).
+        const double tol1 = std::max(toler, 1e-7);
+        for (int s = 0; s < maxit && sweep(MSGPU_MIXED, tol1, err); ++s) {
+        }
+        if (err) return err;
+        for (int r = 0; r < nmed; ++r)
+            for (int i = 0; i < R[r].nr; ++i)
+                if (R[r].flag[i] == 1) R[r].flag[i] = 0;
+                else if (R[r].flag[i] == 0) R[r].flag[i] = -1;  // did not settle in mixed precision
+        for (int s = 0; s < 8 && sweep(MSGPU_FP64, toler, err); ++s) {
+        }
+        if (err) return err;
+    } else {
+        for (int s = 0; s < maxit && sweep(precision, toler, err); ++s) {
+        }
+        if (err) return err;
     }
     for (int r = 0; r < nmed; ++r) {
         Realisation& X = R[r];

@@ -126,6 +126,12 @@ int msgpu_fill_medium(int d, int n, int shape, double ratio, uint64_t seed, doub
     return 0;
 }
 
+// random_double (src/core/nru_random.c:39) n times from init_random(seed)
+void msgpu_random_doubles(uint64_t seed, int n, double* out) {
+    Ran rng(seed);
+    for (int i = 0; i < n; i++) out[i] = rng.uniform();
+}
+
 // get_arg_cmap (src/core/complex_map_util.c:27-31): row-major from the top row
 void msgpu_kplane_args(int nx, int ny, double xmin, double xmax, double ymin, double ymax, double* ks) {
     const double dx = (xmax - xmin) / (nx - 1), dy = (ymax - ymin) / (ny - 1);

@@ -68,3 +68,9 @@ def test_cut_centre_samples_are_the_benchmark_grid():
     centre = ks[4::3][:4096]
     want = 0.5 + 2.5 * np.arange(4096) / 4095 - 0.05j
     assert np.max(np.abs(centre - want)) < 1e-15
+
+
+def test_realisation_sizes_match_reference(ref_runs):
+    import msmodel_gb300 as ms
+    c = [c for c in ref_runs["cases"] if c["kind"] == "realisation_sizes"][0]
+    assert ms.realisation_sizes(len(c["sizes"]), seed=c["seed"]) == c["sizes"]
