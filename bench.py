@@ -249,6 +249,182 @@ def measure_aberth(ms, torch, count, cpu_sample):
     return res
 
 
+# ------------------------------------------------------------------ other configurations
+# Measurement lines for the other configurations of the hot path (one JSON
+# line each, `--workload`); the default line above is the headline.
+
+def _wall(torch, fn):
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return r, time.perf_counter() - t0
+
+
+def _resident(ms, torch, kind, media, ks, precision, steps, warmup, item_med=None):
+    """evals/s of a resident job (inputs in HBM), CUDA events on torch's stream."""
+    job = ms.Job(kind, media, ks, item_med=item_med, precision=precision)
+    st = torch.cuda.current_stream()
+    for _ in range(warmup):
+        job.run(st.cuda_stream)
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        job.run(st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1) * 1e-3
+    out, status = job.results()
+    return len(ks) * steps / tot, out, status
+
+
+def workload_map64(ms, torch, args):
+    """Complex map of ln det M(k)/N, d=3 N=64 seed 1, 64x64 k on [0.5,3] x [-0.5,0]."""
+    med = ms.Medium(3, 64, seed=1)
+    ks = ms.kplane_args(64, 64, 0.5, 3.0, -0.5, 0.0)
+    v64, o64, s64 = _resident(ms, torch, "tracelog", [med], ks, "fp64", args.steps, args.warmup)
+    vmx, omx, smx = _resident(ms, torch, "tracelog", [med], ks, "mixed", args.steps, args.warmup)
+    (_, _), e2e = _wall(torch, lambda: ms.tracelog_batch([med], ks, precision="fp64"))
+    err = np.abs((omx - o64).real) / np.abs(o64.real)
+    line = {"workload": "kplane d=3 N=64 64x64 Re[0.5,3] Im[-0.5,0]", "unit": "evals/s",
+            "fp64": v64, "mixed": vmx, "e2e_fp64": len(ks) / e2e,
+            "mixed_lndet_rel_err": {"max": float(err.max()), "median": float(np.median(err))},
+            "status_nonzero": int(np.count_nonzero(s64) + np.count_nonzero(smx))}
+    if not args.no_cpu:
+        from oracle import Oracle
+        o = Oracle()
+        _, el = _wall(torch, lambda: o.tracelog_batch(3, 64, med.pos, ks, nthreads=os.cpu_count()))
+        ref = o.tracelog_batch(3, 64, med.pos, ks, nthreads=os.cpu_count())
+        line["cpu_baseline"] = {"value": len(ks) / el, "cores": os.cpu_count(), "kind": "port",
+                                "sample": "the whole 4096-point map"}
+        line["fp64_vs_oracle_max_rel"] = float(np.max(np.abs((o64 - ref[0]).real) / np.abs(ref[0].real)))
+    return line
+
+
+def workload_map2d(ms, torch, args):
+    """Complex map d=2 N=2048 seed 1, 256x256 k on [0.5,4] x [-0.3,0]: the mixed
+    engine on the whole map, the FP64 engine on every 16th row and column, and
+    the mixed ln det error against FP64 on that subgrid."""
+    med = ms.Medium(2, 2048, seed=1)
+    ks = ms.kplane_args(256, 256, 0.5, 4.0, -0.3, 0.0)
+    sub = ks.reshape(256, 256)[::16, ::16].reshape(-1).copy()
+    frac = args.sample if args.sample else 1.0
+    kmix = ks[:int(len(ks) * frac)]
+    vmx, omx, smx = _resident(ms, torch, "tracelog", [med], kmix, "mixed", 1, 1)
+    v64, o64, s64 = _resident(ms, torch, "tracelog", [med], sub, "fp64", 1, 1)
+    osub, _ = ms.tracelog_batch([med], sub, precision="mixed")
+    lnd64, lndm = o64 * 2048, osub * 2048
+    err = np.abs(lndm.real - lnd64.real) / np.abs(lnd64.real)
+    return {"workload": f"kplane d=2 N=2048 256x256 Re[0.5,4] Im[-0.3,0] (mixed on {len(kmix)} points)",
+            "unit": "evals/s", "mixed": vmx, "fp64": v64, "ratio": vmx / v64,
+            "mixed_lndet_rel_err_subgrid": {"max": float(err.max()), "median": float(np.median(err)),
+                                            "points": int(err.size)},
+            "im_branch_max_dist": float(np.max(np.abs(((lndm.imag - lnd64.imag) + np.pi) % (2 * np.pi) - np.pi))),
+            "status_nonzero": {"mixed": int(np.count_nonzero(smx)), "fp64": int(np.count_nonzero(s64))}}
+
+
+def workload_aberth(ms, torch, args):
+    """Batched resonance search over realisations 1..count (N from [100,600]):
+    roots/s of the mixed (FP64-finished) search on all of them, the FP64 search
+    on the first `fp64_count`, the root-set agreement there, and the histogram
+    of Im k of every root (40 bins on [-1, 0])."""
+    count = args.count or 4096
+    media = aberth_media(ms, count)
+    z0 = ms.halton_points(ABERTH_DOM, 32)
+    (rm, nem), elm = _wall(torch, lambda: ms.find_eigenstates(media, ABERTH_DOM, 32, 30, 1e-10, "mixed"))
+    nf = min(count, args.fp64_count)
+    (r64, ne64), el64 = _wall(torch, lambda: ms.find_eigenstates(media[:nf], ABERTH_DOM, 32, 30, 1e-10, "fp64"))
+    nrm, nr64 = sum(len(r) for r in rm), sum(len(r) for r in r64)
+    matched = sum(match_count(rm[i], r64[i], 1e-8) for i in range(nf))
+    extra = sum(len(rm[i]) for i in range(nf)) - matched
+    hist, edges = np.histogram(np.concatenate([r.imag for r in rm]) if nrm else np.zeros(0), bins=40,
+                               range=(-1.0, 0.0))
+    line = {"workload": f"aberth d=3 N in [100,600] {count} realisations, 32 Halton seeds",
+            "unit": "roots/s", "mixed": nrm / elm, "mixed_roots": nrm, "mixed_dlogf_evals": nem,
+            "mixed_seconds": elm, "fp64": nr64 / el64, "fp64_realisations": nf, "fp64_roots": nr64,
+            "fp64_seconds": el64, "match_on_fp64_subset": {"matched": matched, "fp64_roots": nr64,
+                                                           "mixed_only": extra},
+            "imag_histogram": {"edges": [float(edges[0]), float(edges[-1])], "counts": hist.tolist()}}
+    if not args.no_cpu:
+        import concurrent.futures as cf
+        from oracle import Oracle
+        o = Oracle()
+        ns = min(count, os.cpu_count() or 1)
+        z0s = z0[np.argsort(-z0.imag, kind="stable")]
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            outs = list(ex.map(lambda m: o.solve_aberth(3, m.n, m.pos, ABERTH_DOM, z0s)[0], media[:ns]))
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": sum(len(r) for r in outs) / el, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"realisations 1..{ns}, one per thread"}
+    return line
+
+
+def workload_wave(ms, torch, args):
+    """Wavefunction d=3 N=4096 seed 1, plane wave along +x at nk real k in
+    [0.5,3], psi on 512x512 pixels of the z=0 plane over [-R,R]^2: solves and
+    grid per second, mixed (refined) and FP64, with the solve residual."""
+    n, nk, npx = 4096, args.nk_wave, 512
+    med = ms.Medium(3, n, seed=1)
+    rad = (n / (4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
+    dom = [-rad, rad, -rad, rad]
+    ks = 0.5 + 2.5 * np.arange(nk) / max(nk - 1, 1) + 0j
+    res = {}
+    for prec in ("mixed", "fp64"):
+        (f, d, _, a), el = _wall(torch, lambda: ms.wave_function_batch([med], ks, npx, npx, dom, prec,
+                                                                       want_psi=False))
+        res[prec] = (f, a[0], el)
+    f_m, a_m, el_m = res["mixed"]
+    f_d, a_d, el_d = res["fp64"]
+    line = {"workload": f"wavefunction d=3 N=4096 {nk} real k in [0.5,3], {npx}x{npx} grid z=0",
+            "unit": "k/s", "mixed": nk / el_m, "fp64": nk / el_d, "mixed_seconds": el_m, "fp64_seconds": el_d,
+            "pair_evals_per_s_mixed": nk * npx * npx * n / el_m,
+            "fun_max_abs_diff_vs_fp64": float(np.max(np.abs(f_m - f_d))),
+            "amp_max_rel_diff_vs_fp64": float(np.max(np.abs(a_m - a_d)) / np.max(np.abs(a_d)))}
+    if not args.no_cpu:
+        from oracle import Oracle
+        o = Oracle()
+        worst = {"mixed": 0.0, "fp64": 0.0}
+        for j in sorted({0, nk // 2, nk - 1}):
+            m = o.ms_matrix(3, n, med.pos, ks[j])
+            phi = np.exp(1j * ks[j] * med.pos[0::3])
+            for prec, a in (("mixed", a_m), ("fp64", a_d)):
+                worst[prec] = max(worst[prec], float(np.max(np.abs(phi - m @ a[j])) / np.max(np.abs(phi))))
+        line["residual_max"] = worst
+        # the reference's per-k cost: the N=4096 solve (2x2 grid) plus the grid (32x32 minus 2x2, per pixel)
+        t0 = time.perf_counter()
+        o.wavefunction(3, n, med.pos, ks[nk // 2], 2, 2, dom, nthreads=os.cpu_count())
+        t_solve = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o.wavefunction(3, n, med.pos, ks[nk // 2], 32, 32, dom, nthreads=os.cpu_count())
+        t_px = max(time.perf_counter() - t0 - t_solve, 0.0) / (32 * 32 - 4)
+        per_k = t_solve + t_px * npx * npx
+        line["cpu_baseline"] = {"value": 1.0 / per_k, "unit": "k/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"one k: N=4096 zgesv {t_solve:.2f} s + {t_px * 1e6:.1f} us per pixel "
+                                          f"(32x32 grid), scaled to {npx}x{npx} pixels"}
+    return line
+
+
+WORKLOADS = {"map64": workload_map64, "map2d": workload_map2d, "aberth": workload_aberth, "wave": workload_wave}
+
+
+def run_workload(args):
+    import torch
+    import msmodel_gb300 as ms
+    torch.cuda.set_device(0)
+    ms.init(0)
+    l0 = ms.launch_count()
+    with Clocks(0) as clk:
+        line = WORKLOADS[args.workload](ms, torch, args)
+    line["gpu_launches"] = ms.launch_count() - l0
+    line["clocks"] = clk.summary()
+    line["data"] = "synthetic (seeded scatterers drawn by the reference's generator)"
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -297,9 +473,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg of an fp64 run")
     ap.add_argument("--aberth", type=int, default=32, help="realisations of the resonance-search leg (0: skip)")
+    ap.add_argument("--workload", default="cut", choices=["cut"] + sorted(WORKLOADS),
+                    help="cut: the headline line; others: one measurement line of that configuration")
+    ap.add_argument("--count", type=int, default=0, help="aberth workload: realisations (default 4096)")
+    ap.add_argument("--fp64-count", type=int, default=64, help="aberth workload: realisations searched in FP64")
+    ap.add_argument("--nk-wave", type=int, default=256, help="wave workload: wave numbers")
+    ap.add_argument("--sample", type=float, default=0.0, help="map2d workload: fraction of the map (default all)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "cut":
+        return run_workload(args)
 
     import torch
     import msmodel_gb300 as ms

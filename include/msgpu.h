@@ -29,6 +29,8 @@ enum { MSGPU_HARDSPHERE = 0, MSGPU_SOFTSPHERE = 1, MSGPU_RESONANT = 2, MSGPU_MAX
 enum { MSGPU_CUBE = 0, MSGPU_BALL = 1, MSGPU_LATTICE = 2, MSGPU_GAUSSIAN = 3 };
 /* Arithmetic of the LU */
 enum { MSGPU_FP64 = 0, MSGPU_MIXED = 1 };
+/* Random functions, enum order of reference src/core/random_function_type.h:18 */
+enum { MSGPU_RF_CRSEC = 0, MSGPU_RF_DOS = 1 };
 
 /* per-result status bits */
 #define MSGPU_S_OK 0
@@ -92,8 +94,10 @@ void msgpu_halton_points(const double* dom, int n, double* z);
  *        1 = dG/dk (dk_free_green, :311), 2 = I_d(k,r) (free_green_imag, :298),
  *        3 = K_{d/2}(k) (bessel_k with twonu = d, :224; r ignored),
  *        4 = F(k)^-1 of *model (invf, src/core/medium_util.c:296; r ignored),
- *        5 = the d = 3 element M_ij = -G(k,r) and 6 = dM_ij/dk as the mixed
- *            engine evaluates them (double-float transcendentals; d ignored) */
+ *        5 = the d = 3 element M_ij = -G(k,r) and 6 = dM_ij/dk with FP64
+ *            distance and reductions, double-float series (d ignored),
+ *        7, 8 = the same two entirely in double-float on the FP32 pipe, as the
+ *            mixed engine assembles d = 3 matrices (r rounded to 48 bits) */
 int msgpu_eval_special(int which, int d, const msgpu_model* model, int n, const double* ks, const double* rs,
                        double* out);
 
@@ -165,6 +169,41 @@ int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, const double* 
  * every medium (n complex each). */
 int msgpu_wave_function(int nmed, const msgpu_medium* media, const double* k, int nx, int ny, const double* dom,
                         double* function, double* density, double* psi, double* amps, int precision);
+/* The same at nk wave numbers ks[2*nk] (one solve per medium and k, all in
+ * one batched job): function/density[nk*nx*ny] and psi[nk*nx*ny] (complex,
+ * media[0]) are k-major, amps[nmed][nk][n].  MSGPU_MIXED solves with the
+ * mixed engine plus FP64-residual refinement and, for d = 3, evaluates the
+ * Green functions of the grid in double-float arithmetic on the FP32 pipe
+ * (|Im k| * r < 80 over the grid; otherwise FP64). */
+int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, int nk, const double* ks, int nx, int ny,
+                              const double* dom, double* function, double* density, double* psi, double* amps,
+                              int precision);
+
+/* Random function of run_random_function_omp (src/core/ms_core.c:476-519):
+ * for every seed g < nseed (medium filled with seed g+1 by fill_medium) and
+ * every bin i < nbin, k_i = xmin exp(i log(xmax/xmin)/(nbin-1))
+ * (random_function_util.c:103), the total cross section
+ * (MSGPU_RF_CRSEC, ms_matrix_util.c:344) or the density of states
+ * -Im dlogf(k_i)/(2 pi k_i) (MSGPU_RF_DOS) into data[g + i*nseed]; each bin's
+ * nseed samples then sorted ascending (sort_random_function,
+ * random_function_util.c:110).  status (may be NULL) per sample, same
+ * layout before sorting. */
+int msgpu_random_function(int type, int d, int n, int shape, double ratio, const msgpu_model* model, int nseed,
+                          int nbin, double xmin, double xmax, double* data, int* status, int precision);
+
+/* Launch choices (autotuning).  Per (kind, requested precision, size bucket
+ * of the job's largest n: (2^(b-1), 2^b]) the engine that runs and the
+ * resident CTAs per SM of the persistent grid.  engine: MSGPU_FP64,
+ * MSGPU_MIXED (only for a mixed request) or -1 = the requested one; ctas 0 =
+ * as many as fit.  The FP64 engine may serve a mixed request: it meets the
+ * mixed accuracy bound with room to spare. */
+int msgpu_tune_set(int kind, int precision, int n, int engine, int ctas_per_sm);
+int msgpu_tune_get(int kind, int precision, int n, int* engine, int* ctas_per_sm);
+/* Time every candidate (engine x 1 or 2 CTAs per SM) on a probe batch of
+ * nitem k for n scatterers of d dimensions (the reference ball, seed 1) and
+ * keep the fastest for that size bucket.  seconds[4] receives the times
+ * (fp64 x1, fp64 x2, mixed x1, mixed x2; -1 where not run). */
+int msgpu_autotune(int kind, int precision, int d, int n, int nitem, double* seconds);
 
 /* Resident jobs: inputs uploaded once, the hot path run on device-resident
  * data (asynchronously on `stream`, a cudaStream_t or NULL), results fetched
@@ -173,6 +212,14 @@ typedef struct msgpu_job msgpu_job;
 msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
                             const double* ks, int precision);
 int msgpu_job_run(msgpu_job* job, void* stream);
+/* Replace the job's items (nitem <= the count it was created with) keeping
+ * its media resident: the next run evaluates these points. */
+int msgpu_job_set_points(msgpu_job* job, int nitem, const int* item_med, const double* ks);
+/* on != 0: msgpu_job_run replays a CUDA graph of the run (queue reset plus
+ * the persistent engine launch), captured on first use and recaptured only if
+ * the library's shared workspace moved; set_points needs no recapture (the
+ * engine reads the live item count from device memory). */
+int msgpu_job_use_graph(msgpu_job* job, int on);
 int msgpu_job_results(msgpu_job* job, double* out, int* status);
 int msgpu_job_amplitudes(msgpu_job* job, double* amps);
 /* kernels launched by one msgpu_job_run */

@@ -51,6 +51,19 @@ typedef struct msgpu_ref_cdata {
     msgpu_dcomplex (*get_arg)(void* self, int i);
 } msgpu_ref_cdata;
 
+/* reference RandomFunction, src/core/random_function_type.h:22-33 */
+typedef struct msgpu_ref_rfun {
+    int type; /* 0 = crsec, 1 = dos */
+    int nbin;
+    int nseed;
+    int ntot;
+    double xmin;
+    double xmax;
+    double* data;
+    char title[80];
+    double realtime;
+} msgpu_ref_rfun;
+
 /* replaces build_ms_matrix, src/core/ms_matrix_util.c:32 */
 void build_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix);
 /* replaces build_dk_ms_matrix, src/core/ms_matrix_util.c:68 */
@@ -67,6 +80,10 @@ double total_cross_section(msgpu_ref_medium* med, double k);
  * task in one batched GPU job; the seeds are filled with the reference's
  * generator (seed s = 1..nseed), data[] is the same running average. */
 void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread);
+/* replaces run_random_function_omp, src/core/ms_core.c:476: every (seed, bin)
+ * sample in one batched GPU job, bins sorted; the medium is left filled with
+ * the last seed, as the reference leaves it */
+void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nthread);
 
 #ifdef __cplusplus
 }

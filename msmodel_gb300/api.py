@@ -68,6 +68,8 @@ def lib():
     L.msgpu_job_run.argtypes = [C.c_void_p, C.c_void_p]
     L.msgpu_job_results.argtypes = [C.c_void_p, _dp, _ip]
     L.msgpu_job_amplitudes.argtypes = [C.c_void_p, _dp]
+    L.msgpu_job_set_points.argtypes = [C.c_void_p, C.c_int, C.c_void_p, _dp]
+    L.msgpu_job_use_graph.argtypes = [C.c_void_p, C.c_int]
     L.msgpu_job_launches.argtypes = [C.c_void_p]
     L.msgpu_job_flops.argtypes = [C.c_void_p]
     L.msgpu_job_flops.restype = C.c_double
@@ -75,6 +77,13 @@ def lib():
     L.msgpu_engine_stats.argtypes = [_dp, C.c_int]
     L.msgpu_wave_function.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, C.c_int, _dp, _dp, _dp, C.c_void_p,
                                        C.c_void_p, C.c_int]
+    L.msgpu_wave_function_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _dp, C.c_int, C.c_int, _dp, _dp,
+                                             _dp, C.c_void_p, C.c_void_p, C.c_int]
+    L.msgpu_random_function.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(_Model), C.c_int,
+                                         C.c_int, C.c_double, C.c_double, _dp, _ip, C.c_int]
+    L.msgpu_tune_set.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.msgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.msgpu_autotune.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
     L.msgpu_solve_aberth_batch.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, _dp, C.c_int, C.c_int,
                                            C.c_double, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
     _lib = L
@@ -342,6 +351,25 @@ def total_cross_section(med, k):
     return float(sig[0].real)
 
 
+RANDOM_FUNCTIONS = {"crsec": 0, "dos": 1}
+
+
+def random_function(kind, d, n, nseed, nbin, xmin, xmax, model="maximum", params=(), shape="ball", ratio=1.0,
+                    precision="fp64"):
+    """run_random_function_omp (ms_core.c:476-519): total cross section
+    ("crsec") or density of states ("dos") for seeds 1..nseed at the nbin
+    log-spaced real k of get_arg_rfun (random_function_util.c:103), every bin
+    sorted.  Returns (k[nbin], data[nbin, nseed], status[nbin*nseed])."""
+    data = np.zeros(nseed * nbin)
+    status = np.zeros(nseed * nbin, dtype=np.int32)
+    m = _model(model, params)
+    _check(lib().msgpu_random_function(RANDOM_FUNCTIONS[kind], d, n, SHAPES[shape] if isinstance(shape, str) else shape,
+                                       ratio, C.byref(m), nseed, nbin, xmin, xmax, data, status,
+                                       PRECISION[precision]), "random_function")
+    ks = xmin * np.exp(np.arange(nbin) * np.log(xmax / xmin) / (nbin - 1))
+    return ks, data.reshape(nbin, nseed), status
+
+
 def run_tracelog(d, n, ks, nseed=1, model="maximum", params=(), shape="ball", ratio=1.0, precision="fp64"):
     """The k-point loop of run_tracelog_omp (ms_core.c:96-141): seeds 1..nseed,
     ln det/n at every k, averaged over seeds in seed order."""
@@ -360,17 +388,29 @@ def run_tracelog(d, n, ks, nseed=1, model="maximum", params=(), shape="ball", ra
 def wave_function(media, k, nx, ny, dom, precision="fp64"):
     """run_wave_function_omp (ms_core.c:596): seed-averaged Re psi and |psi|^2 on
     the nx x ny grid, plus psi of the first medium and every medium's amplitudes."""
+    fun, den, psi, amps = wave_function_batch(media, [k], nx, ny, dom, precision)
+    return fun[0], den[0], psi[0], [a[0] for a in amps]
+
+
+def wave_function_batch(media, ks, nx, ny, dom, precision="fp64", want_psi=True):
+    """run_wave_function_omp at every k of ks, all solves in one batched job.
+    Returns fun[nk, nx*ny], den[nk, nx*ny], psi[nk, nx*ny] of the first medium
+    (None unless want_psi), amps[medium][k] (n complex each)."""
     media = [media] if isinstance(media, Medium) else list(media)
-    fun = np.zeros(nx * ny)
-    den = np.zeros(nx * ny)
-    psi = np.zeros(2 * nx * ny)
-    amps = np.zeros(2 * sum(m.n for m in media))
+    ks = np.ascontiguousarray(np.asarray(ks, dtype=np.complex128))
+    nk, n, npx = len(ks), media[0].n, nx * ny
+    fun = np.zeros(nk * npx)
+    den = np.zeros(nk * npx)
+    psi = np.zeros(2 * nk * npx) if want_psi else None
+    amps = np.zeros(2 * len(media) * nk * n)
     arr = _media_array(media)
-    _check(lib().msgpu_wave_function(len(media), arr, _c2(k), nx, ny, np.asarray(dom, dtype=np.float64), fun, den,
-                                     psi.ctypes.data, amps.ctypes.data, PRECISION[precision]), "wave_function")
-    a = amps.view(np.complex128)
-    n = media[0].n
-    return fun, den, psi.view(np.complex128).copy(), [a[i * n:(i + 1) * n].copy() for i in range(len(media))]
+    _check(lib().msgpu_wave_function_batch(len(media), arr, nk, ks.view(np.float64), nx, ny,
+                                           np.asarray(dom, dtype=np.float64), fun, den,
+                                           psi.ctypes.data if want_psi else None, amps.ctypes.data,
+                                           PRECISION[precision]), "wave_function_batch")
+    a = amps.view(np.complex128).reshape(len(media), nk, n)
+    return (fun.reshape(nk, npx), den.reshape(nk, npx),
+            psi.view(np.complex128).reshape(nk, npx) if want_psi else None, [a[m].copy() for m in range(len(media))])
 
 
 def solve_aberth_batch(media, dom, z0, nexpsup=4, maxit=30, toler=1e-10, precision="fp64"):
@@ -400,6 +440,60 @@ def find_eigenstates(media, dom, ntarget, maxit=30, toler=1e-10, precision="fp64
     return [r[np.argsort(-r.imag, kind="stable")] for r in roots], ne
 
 
+# --------------------------------------------------------------------------- autotuning
+KIND_CODES = {"tracelog": 0, "dlogf": 1, "amplitude": 2}
+ENGINES = {-1: None, 0: "fp64", 1: "mixed"}
+
+
+def tune_set(kind, precision, n, engine=None, ctas_per_sm=0):
+    """Fix the launch choice for jobs of this kind and requested precision whose
+    largest n falls in n's size bucket (engine None = the requested one)."""
+    e = -1 if engine is None else PRECISION[engine]
+    _check(lib().msgpu_tune_set(KIND_CODES[kind], PRECISION[precision], n, e, ctas_per_sm), "tune_set")
+
+
+def tune_get(kind, precision, n):
+    e, c = C.c_int(0), C.c_int(0)
+    _check(lib().msgpu_tune_get(KIND_CODES[kind], PRECISION[precision], n, C.byref(e), C.byref(c)), "tune_get")
+    return ENGINES[e.value], c.value
+
+
+def autotune(kind, precision, d, n, nitem=None):
+    """Time the candidate launches (engine x CTAs per SM) on a probe batch and
+    keep the fastest for n's size bucket.  Returns {candidate: seconds} and the
+    choice."""
+    nitem = nitem or 2 * sm_count()
+    t = np.full(4, -1.0)
+    _check(lib().msgpu_autotune(KIND_CODES[kind], PRECISION[precision], d, n, nitem, t), "autotune")
+    names = ["fp64 x1", "fp64 x2", "mixed x1", "mixed x2"]
+    return {names[i]: float(t[i]) for i in range(4) if t[i] >= 0}, tune_get(kind, precision, n)
+
+
+def tune_table():
+    """Every non-default entry: [(kind, precision, bucket upper n, engine, ctas)]."""
+    rows = []
+    for kind in KIND_CODES:
+        for prec in PRECISION:
+            for b in range(17):
+                e, c = tune_get(kind, prec, 1 << b)
+                if e is not None or c:
+                    rows.append((kind, prec, 1 << b, e, c))
+    return rows
+
+
+def tune_save(path):
+    import json
+    with open(path, "w") as f:
+        json.dump(tune_table(), f)
+
+
+def tune_load(path):
+    import json
+    with open(path) as f:
+        for kind, prec, n, e, c in json.load(f):
+            tune_set(kind, prec, n, e, c)
+
+
 class Job:
     """A resident job: inputs on the device, run asynchronously on a stream
     (the handle of a CUDA stream, e.g. torch.cuda.current_stream().cuda_stream)."""
@@ -420,6 +514,17 @@ class Job:
 
     def run(self, stream=None):
         _check(lib().msgpu_job_run(self.h, stream), "job_run")
+
+    def set_points(self, ks, item_med=None):
+        """Replace the items (at most the count the job was created with); the
+        media stay resident."""
+        kk, nitem, im = _items(self.media, ks, item_med)
+        _check(lib().msgpu_job_set_points(self.h, nitem, im.ctypes.data, kk), "job_set_points")
+        self.nitem, self._keep, self.item_med = nitem, (kk, im), im
+
+    def use_graph(self, on=True):
+        """Replay the run as a captured CUDA graph."""
+        _check(lib().msgpu_job_use_graph(self.h, int(on)), "job_use_graph")
 
     def results(self):
         out = np.zeros(2 * self.nitem)

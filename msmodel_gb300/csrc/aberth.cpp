@@ -104,6 +104,35 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
         R[r].aborted = R[r].nr <= 1;
     }
     const int deg = nexpsup - 1;
+    // One resident dlogf job per precision serves every evaluation of the
+    // search: the media are uploaded once, each batch replaces the points and
+    // replays the captured run.
+    struct Jobs {
+        msgpu_job* j[2] = {nullptr, nullptr};
+        ~Jobs() {
+            msgpu_job_destroy(j[0]);
+            msgpu_job_destroy(j[1]);
+        }
+    } jobs;
+    const int cap = nmed * std::max(std::max(nz, 6 * nexpsup), 1);
+    auto dlogf_batch = [&](int prec, const std::vector<int>& im, const std::vector<double>& ks, std::vector<double>& out,
+                           std::vector<int>& st) -> int {
+        msgpu_job*& J = jobs.j[prec == MSGPU_MIXED ? 1 : 0];
+        if (!J) {
+            std::vector<int> fim(cap);
+            std::vector<double> fks(2 * (size_t)cap, 0.0);
+            for (int i = 0; i < cap; ++i) {
+                fim[i] = i % nmed;
+                fks[2 * i] = 1.0;
+            }
+            J = msgpu_job_create(1, nmed, media, cap, fim.data(), fks.data(), prec);
+            if (!J) return MSGPU_E_CUDA;
+            if (int e = msgpu_job_use_graph(J, 1)) return e;
+        }
+        if (int e = msgpu_job_set_points(J, (int)im.size(), im.data(), ks.data())) return e;
+        if (int e = msgpu_job_run(J, nullptr)) return e;
+        return msgpu_job_results(J, out.data(), st.data());
+    };
     if (nexpsup > 0) {
         const int ns = 6 * nexpsup;
         std::vector<double> hz(2 * ns);
@@ -121,8 +150,7 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
         if (!im.empty()) {
             std::vector<double> out(ks.size());
             std::vector<int> st(im.size());
-            int e = msgpu_dk_log_det_batch(nmed, media, (int)im.size(), im.data(), ks.data(), out.data(), st.data(),
-                                           precision);
+            int e = dlogf_batch(precision, im, ks, out, st);
             if (e) return e;
             ne += (long long)im.size();
             size_t q = 0;
@@ -159,7 +187,7 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
         if (im.empty()) return false;
         std::vector<double> out(ks.size());
         std::vector<int> st(im.size());
-        err = msgpu_dk_log_det_batch(nmed, media, (int)im.size(), im.data(), ks.data(), out.data(), st.data(), prec);
+        err = dlogf_batch(prec, im, ks, out, st);
         if (err) return false;
         ne += (long long)im.size();
         size_t q = 0;

@@ -138,3 +138,19 @@ void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread
     cdata->realtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
     free(media); free(pos); free(ks); free(im); free(out);
 }
+
+void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nthread) {
+    (void)nthread;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    msgpu_model mdl = to_model(med->scmodel);
+    int e = msgpu_random_function(rfun->type, med->d, med->n, med->shape, med->ratio, &mdl, rfun->nseed, rfun->nbin,
+                                  rfun->xmin, rfun->xmax, rfun->data, NULL, MSGPU_FP64);
+    if (e) fail("run_random_function_omp", e);
+    if (rfun->nseed > 0) {
+        e = msgpu_fill_medium(med->d, med->n, med->shape, med->ratio, (uint64_t)rfun->nseed, med->pos);
+        if (e) fail("run_random_function_omp: fill_medium", e);
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    rfun->realtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+}

@@ -40,7 +40,8 @@ __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
     int* ipiv = P.piv + (size_t)blockIdx.x * P.piv_stride;
     for (;;) {
         if (threadIdx.x == 0) {
-            s.item = (int)atomicAdd(P.counter, 1u);
+            const unsigned q = atomicAdd(P.counter, 1u);
+            s.item = q < P.counter[1] ? (int)q : P.nitem;
             s.info = 0;
         }
         __syncthreads();
@@ -148,6 +149,11 @@ __global__ void __launch_bounds__(NT, 1) k_tracelog_matrix(zc* A, int n, int* ip
 
 __global__ void k_eval_special(int which, int d, msgpu_model m, int n, const double* ks, const double* rs,
                                double* out) {
+    __shared__ Df3Tables tab;
+    if (which >= 7) {  // block-uniform
+        df3_tables_init(tab);
+        __syncthreads();
+    }
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     zc k = mk(ks[2 * i], ks[2 * i + 1]);
@@ -166,14 +172,23 @@ __global__ void k_eval_special(int which, int d, msgpu_model m, int n, const dou
         v = mk(df_to_double(e.re), df_to_double(e.im));
         break;
     }
+    case 7:
+    case 8: {  // the same elements entirely on the FP32 pipe, as the mixed engine assembles them
+        dfc a, b;
+        pair_elements_df3t(tab, df_from_double(k.re), df_from_double(k.im), k.im != 0.0, df_from_double(r),
+                           which == 8, a, b);
+        const dfc e = which == 7 ? a : b;
+        v = mk(df_to_double(e.re), df_to_double(e.im));
+        break;
+    }
     default: v = invf(m, d, k); break;
     }
     out[2 * i] = v.re;
     out[2 * i + 1] = v.im;
 }
 
-// FP64 FMA throughput probe: 8 independent chains per thread.  MEASURED_PEAKS
-// carries no FP64 figure, so the plain path's roofline denominator is this.
+// FP64 FMA throughput probe: 8 independent chains per thread; the roofline
+// denominator of the plain (FP64-pipe-bound) path.
 __global__ void k_probe_dfma(double* sink, int iters, double a, double b) {
     double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
            x7 = x0 + 7;
@@ -200,6 +215,25 @@ int g_ctas_fp64 = 0;
 std::atomic<uint64_t> g_launches{0};
 void* g_ws = nullptr;
 size_t g_ws_bytes = 0;
+unsigned long long g_ws_gen = 1;  // changes whenever g_ws moves (captured graphs hold its address)
+
+// Launch choices per (kind, requested precision, size bucket): the engine that
+// runs (a mixed request may be served by the FP64 engine, which is at least as
+// accurate) and the resident CTAs per SM of the persistent grid.  0 = default
+// (the requested engine, as many CTAs as fit).  Filled by msgpu_autotune or
+// msgpu_tune_set; bucket b holds nmax in (2^(b-1), 2^b].
+struct TuneEntry {
+    int engine = 0;  // 0 default, 1 + MSGPU_FP64 / 1 + MSGPU_MIXED
+    int ctas = 0;
+};
+constexpr int TUNE_BUCKETS = 17;
+TuneEntry g_tune[3][2][TUNE_BUCKETS];
+
+int size_bucket(int n) {
+    int b = 0;
+    while ((1 << b) < n && b < TUNE_BUCKETS - 1) ++b;
+    return b;
+}
 
 int set_err(int code, const std::string& msg) {
     g_err = msg;
@@ -238,6 +272,7 @@ int ensure_ws(size_t bytes, void** p) {
         if (g_ws) cudaFree(g_ws);
         g_ws = nullptr;
         g_ws_bytes = 0;
+        ++g_ws_gen;
         CK(cudaMalloc(&g_ws, bytes));
         g_ws_bytes = bytes;
     }
@@ -258,8 +293,10 @@ static size_t ws_budget() {
 
 struct msgpu_job {
     int kind = 0, precision = 0, nitem = 0, nmed = 0, nmax = 0;
+    int cap = 0;  // item capacity of the device arrays
     double flops = 0.0;
     int grid = 0;
+    std::vector<int> med_n;  // n of every medium (host copy)
     MedDev* d_media = nullptr;
     double* d_pos = nullptr;
     double* d_ks = nullptr;
@@ -267,13 +304,18 @@ struct msgpu_job {
     int* d_order = nullptr;
     double* d_out = nullptr;
     int* d_status = nullptr;
-    unsigned* d_counter = nullptr;
+    unsigned* d_counter = nullptr;  // [0] work queue, [1] live items
     int* d_piv = nullptr;
     size_t slot = 0;
     size_t ws_bytes = 0;
-    long long amp_total = 0;
+    long long amp_total = 0, amp_cap = 0;
     double* d_amps = nullptr;
     long long* d_amp_off = nullptr;
+    // graph mode: the run (queue reset + engine launch) captured once and replayed
+    bool use_graph = false;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned long long gen = 0;
 };
 
 extern "C" {
@@ -394,6 +436,42 @@ int msgpu_tracelog_matrix(int n, const double* mat, double* out, int* info) {
     return 0;
 }
 
+// Items of a job: medium of each, k, the queue order (largest matrices
+// first), the amplitude offsets (kind 2), the live count.  Caller holds g_mu.
+static int set_items_locked(msgpu_job* J, int nitem, const int* item_med, const double* ks) {
+    if (nitem < 1 || nitem > J->cap || !ks) return set_err(MSGPU_E_ARG, "job: bad item count");
+    std::vector<int> med_of(nitem);
+    double flops = 0.0;
+    long long amp_total = 0;
+    for (int i = 0; i < nitem; i++) {
+        const int mi = item_med ? item_med[i] : 0;
+        if (mi < 0 || mi >= J->nmed) return set_err(MSGPU_E_ARG, "job: bad item medium");
+        med_of[i] = mi;
+        const double n = J->med_n[mi], n3 = n * n * n, n2 = n * n;
+        flops += (J->kind == 0) ? 8.0 / 3.0 * n3 : (J->kind == 1 ? (8.0 / 3.0 + 8.0) * n3 : 8.0 / 3.0 * n3 + 8.0 * n2);
+        amp_total += J->med_n[mi];
+    }
+    if (J->kind == 2 && J->d_amps && amp_total > J->amp_cap) return set_err(MSGPU_E_SIZE, "job: amplitudes exceed capacity");
+    std::vector<int> order(nitem);
+    for (int i = 0; i < nitem; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return J->med_n[med_of[a]] > J->med_n[med_of[b]]; });
+    CK(cudaMemcpy(J->d_ks, ks, sizeof(double) * 2 * nitem, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(J->d_item_med, med_of.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(J->d_order, order.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice));
+    if (J->kind == 2 && J->d_amp_off) {
+        std::vector<long long> off(nitem);
+        long long acc = 0;
+        for (int i = 0; i < nitem; i++) { off[i] = acc; acc += J->med_n[med_of[i]]; }
+        CK(cudaMemcpy(J->d_amp_off, off.data(), sizeof(long long) * nitem, cudaMemcpyHostToDevice));
+    }
+    const unsigned live = (unsigned)nitem;
+    CK(cudaMemcpy(J->d_counter + 1, &live, sizeof(unsigned), cudaMemcpyHostToDevice));
+    J->nitem = nitem;
+    J->flops = flops;
+    J->amp_total = amp_total;
+    return 0;
+}
+
 msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
                             const double* ks, int precision) {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -409,8 +487,9 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     auto* J = new msgpu_job();
     J->kind = kind;
     J->precision = precision;
-    J->nitem = nitem;
+    J->cap = nitem;
     J->nmed = nmed;
+    J->med_n.resize(nmed);
     std::vector<MedDev> hm(nmed);
     size_t npos = 0;
     for (int i = 0; i < nmed; i++) {
@@ -421,26 +500,9 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
             return nullptr;
         }
         J->nmax = std::max(J->nmax, m.n);
+        J->med_n[i] = m.n;
         npos += (size_t)m.n * m.d;
     }
-    std::vector<int> med_of(nitem);
-    for (int i = 0; i < nitem; i++) {
-        int mi = item_med ? item_med[i] : 0;
-        if (mi < 0 || mi >= nmed) {
-            set_err(MSGPU_E_ARG, "job: bad item medium");
-            delete J;
-            return nullptr;
-        }
-        med_of[i] = mi;
-        double n3 = (double)media[mi].n * media[mi].n * media[mi].n;
-        double n2 = (double)media[mi].n * media[mi].n;
-        J->flops += (kind == 0) ? 8.0 / 3.0 * n3 : (kind == 1 ? (8.0 / 3.0 + 8.0) * n3 : 8.0 / 3.0 * n3 + 8.0 * n2);
-        J->amp_total += media[mi].n;
-    }
-    // largest matrices first
-    std::vector<int> order(nitem);
-    for (int i = 0; i < nitem; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return media[med_of[a]].n > media[med_of[b]].n; });
     auto fail = [&](const char* what) -> msgpu_job* {
         set_err(MSGPU_E_CUDA, std::string("job: ") + what);
         msgpu_job_destroy(J);
@@ -454,14 +516,12 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     if (cudaMalloc(&J->d_out, sizeof(double) * 2 * nitem) != cudaSuccess) return fail("alloc out");
     if (cudaMalloc(&J->d_status, sizeof(int) * nitem) != cudaSuccess) return fail("alloc status");
     if (cudaMalloc(&J->d_counter, 256) != cudaSuccess) return fail("alloc counter");
+    if (cudaMemset(J->d_counter, 0, 256) != cudaSuccess) return fail("clear counter");
     if (kind == 2) {
-        std::vector<long long> off(nitem);
-        long long acc = 0;
-        for (int i = 0; i < nitem; i++) { off[i] = acc; acc += media[med_of[i]].n; }
-        if (cudaMalloc(&J->d_amps, sizeof(double) * 2 * (size_t)acc) != cudaSuccess) return fail("alloc amps");
+        // capacity for the amplitudes of nitem items of the largest medium
+        J->amp_cap = (long long)nitem * J->nmax;
+        if (cudaMalloc(&J->d_amps, sizeof(double) * 2 * (size_t)J->amp_cap) != cudaSuccess) return fail("alloc amps");
         if (cudaMalloc(&J->d_amp_off, sizeof(long long) * nitem) != cudaSuccess) return fail("alloc amp_off");
-        if (cudaMemcpy(J->d_amp_off, off.data(), sizeof(long long) * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
-            return fail("copy amp_off");
     }
     size_t off = 0;
     for (int i = 0; i < nmed; i++) {
@@ -474,16 +534,17 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     }
     if (cudaMemcpy(J->d_media, hm.data(), sizeof(MedDev) * nmed, cudaMemcpyHostToDevice) != cudaSuccess)
         return fail("copy media");
-    if (cudaMemcpy(J->d_ks, ks, sizeof(double) * 2 * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
-        return fail("copy ks");
-    if (cudaMemcpy(J->d_item_med, med_of.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
-        return fail("copy items");
-    if (cudaMemcpy(J->d_order, order.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) != cudaSuccess)
-        return fail("copy order");
+    if (set_items_locked(J, nitem, item_med, ks)) {
+        msgpu_job_destroy(J);
+        return nullptr;
+    }
     // per-CTA slots
     J->slot = (size_t)J->nmax * J->nmax;
     const size_t per_cta = slot_elems(kind, J->slot, J->nmax) * sizeof(zc);
-    int grid = std::min(nitem, g_sms * g_ctas_fp64);
+    const TuneEntry& te = g_tune[kind][precision][size_bucket(J->nmax)];
+    if (te.engine) J->precision = te.engine - 1;
+    const int ctas = te.ctas ? std::min(te.ctas, g_ctas_fp64) : g_ctas_fp64;
+    int grid = std::min(nitem, g_sms * ctas);
     size_t budget = ws_budget();
     while (grid > 1 && (size_t)grid * per_cta > budget) grid--;
     J->grid = grid;
@@ -497,19 +558,28 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     return J;
 }
 
-int msgpu_job_run(msgpu_job* J, void* stream) {
+int msgpu_job_set_points(msgpu_job* J, int nitem, const int* item_med, const double* ks) {
     if (!J) return set_err(MSGPU_E_ARG, "null job");
     std::lock_guard<std::mutex> lk(g_mu);
-    cudaStream_t st = (cudaStream_t)stream;
-    void* ws = nullptr;
-    if (int e = ensure_ws(J->ws_bytes, &ws)) return e;
+    return set_items_locked(J, nitem, item_med, ks);
+}
+
+int msgpu_job_use_graph(msgpu_job* J, int on) {
+    if (!J) return set_err(MSGPU_E_ARG, "null job");
+    std::lock_guard<std::mutex> lk(g_mu);
+    J->use_graph = on != 0;
+    return 0;
+}
+
+// the work of one run on stream st: reset the queue, launch the engine
+static int launch_locked(msgpu_job* J, void* ws, cudaStream_t st) {
     CK(cudaMemsetAsync(J->d_counter, 0, sizeof(unsigned), st));
     EngineParams P;
     P.media = J->d_media;
     P.ks = J->d_ks;
     P.item_med = J->d_item_med;
     P.order = J->d_order;
-    P.nitem = J->nitem;
+    P.nitem = J->cap;
     P.ws = reinterpret_cast<zc*>(ws);
     P.slot = J->slot;
     P.piv = J->d_piv;
@@ -522,12 +592,48 @@ int msgpu_job_run(msgpu_job* J, void* stream) {
     P.amp_off = J->d_amp_off;
     if (J->precision == MSGPU_MIXED) {
         int e = mixed_run(P, J->grid, J->nmax, st);
-        g_launches += mixed_launches();
-        return e;
+        if (e) return set_err(e, "mixed engine launch failed");
+        return 0;
     }
     k_engine_fp64<<<J->grid, NT, smem_bytes(), st>>>(P);
-    g_launches++;
     CK(cudaGetLastError());
+    return 0;
+}
+
+int msgpu_job_run(msgpu_job* J, void* stream) {
+    if (!J) return set_err(MSGPU_E_ARG, "null job");
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    void* ws = nullptr;
+    if (int e = ensure_ws(J->ws_bytes, &ws)) return e;
+    if (!J->use_graph) {
+        if (int e = launch_locked(J, ws, st)) return e;
+        g_launches++;
+        return 0;
+    }
+    if (J->precision == MSGPU_MIXED && mixed_prepare(J->grid, J->nmax)) return set_err(MSGPU_E_CUDA, "mixed scratch");
+    const unsigned long long gen = g_ws_gen * 0x9E3779B97F4A7C15ULL + mixed_generation();
+    if (!J->gexec || J->gen != gen) {
+        // (re)capture: the graph holds the workspace and scratch addresses
+        if (J->gexec) cudaGraphExecDestroy(J->gexec);
+        J->gexec = nullptr;
+        if (!J->cap_stream) CK(cudaStreamCreateWithFlags(&J->cap_stream, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(J->cap_stream, cudaStreamCaptureModeRelaxed));
+        const int e = launch_locked(J, ws, J->cap_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(J->cap_stream, &g);
+        if (e) {
+            if (g) cudaGraphDestroy(g);
+            return e;
+        }
+        CK(ce);
+        const cudaError_t ie = cudaGraphInstantiate(&J->gexec, g, 0);
+        cudaGraphDestroy(g);
+        CK(ie);
+        J->gen = gen;
+    }
+    CK(cudaGraphLaunch(J->gexec, st));
+    g_launches++;
     return 0;
 }
 
@@ -553,6 +659,8 @@ int msgpu_job_amplitudes(msgpu_job* J, double* amps) {
 
 void msgpu_job_destroy(msgpu_job* J) {
     if (!J) return;
+    if (J->gexec) cudaGraphExecDestroy(J->gexec);
+    if (J->cap_stream) cudaStreamDestroy(J->cap_stream);
     cudaFree(J->d_media);
     cudaFree(J->d_pos);
     cudaFree(J->d_ks);
@@ -565,6 +673,85 @@ void msgpu_job_destroy(msgpu_job* J) {
     cudaFree(J->d_amps);
     cudaFree(J->d_amp_off);
     delete J;
+}
+
+int msgpu_tune_set(int kind, int precision, int n, int engine, int ctas_per_sm) {
+    if (kind < 0 || kind > 2 || (precision != MSGPU_FP64 && precision != MSGPU_MIXED) || n < 1 ||
+        (engine != -1 && engine != MSGPU_FP64 && engine != MSGPU_MIXED) || ctas_per_sm < 0 || ctas_per_sm > 8)
+        return set_err(MSGPU_E_ARG, "tune_set: bad argument");
+    if (precision == MSGPU_FP64 && engine == MSGPU_MIXED)
+        return set_err(MSGPU_E_ARG, "tune_set: an FP64 request cannot run on the mixed engine");
+    std::lock_guard<std::mutex> lk(g_mu);
+    TuneEntry& e = g_tune[kind][precision][size_bucket(n)];
+    e.engine = engine < 0 ? 0 : engine + 1;
+    e.ctas = ctas_per_sm;
+    return 0;
+}
+
+int msgpu_tune_get(int kind, int precision, int n, int* engine, int* ctas_per_sm) {
+    if (kind < 0 || kind > 2 || (precision != MSGPU_FP64 && precision != MSGPU_MIXED) || n < 1 || !engine ||
+        !ctas_per_sm)
+        return set_err(MSGPU_E_ARG, "tune_get: bad argument");
+    std::lock_guard<std::mutex> lk(g_mu);
+    const TuneEntry& e = g_tune[kind][precision][size_bucket(n)];
+    *engine = e.engine - 1;
+    *ctas_per_sm = e.ctas;
+    return 0;
+}
+
+int msgpu_autotune(int kind, int precision, int d, int n, int nitem, double* seconds) {
+    if (kind < 0 || kind > 2 || (precision != MSGPU_FP64 && precision != MSGPU_MIXED) || d < 2 || d > 3 ||
+        n < 2 || nitem < 1 || !seconds)
+        return set_err(MSGPU_E_ARG, "autotune: bad argument");
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (int e = init_locked(-1)) return e;
+    }
+    // probe: n scatterers of the reference's ball (seed 1), nitem k on the
+    // real axis ... -0.05i (cross sections need real k)
+    std::vector<double> pos((size_t)n * d), ks(2 * (size_t)nitem);
+    if (int e = msgpu_fill_medium(d, n, MSGPU_BALL, 1.0, 1, pos.data())) return e;
+    for (int i = 0; i < nitem; ++i) {
+        ks[2 * i] = 0.5 + 2.5 * i / std::max(1, nitem - 1);
+        ks[2 * i + 1] = kind == 2 ? 0.0 : -0.05;
+    }
+    const msgpu_medium med{d, n, pos.data(), {MSGPU_MAXIMUM, 0, {0.0, 0.0}}};
+    const int engines[2] = {MSGPU_FP64, MSGPU_MIXED};
+    double best = 0.0;
+    int best_e = precision, best_c = 0;
+    for (int ei = 0; ei < (precision == MSGPU_MIXED ? 2 : 1); ++ei)
+        for (int c = 1; c <= 2; ++c) {
+            const int eng = precision == MSGPU_MIXED ? engines[ei] : MSGPU_FP64;
+            double& t = seconds[ei * 2 + (c - 1)];
+            t = -1.0;
+            if (c > g_ctas_fp64) continue;
+            if (int e = msgpu_tune_set(kind, precision, n, eng, c)) return e;
+            msgpu_job* J = msgpu_job_create(kind, 1, &med, nitem, nullptr, ks.data(), precision);
+            if (!J) return MSGPU_E_CUDA;
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            int err = msgpu_job_run(J, nullptr);  // warm-up (allocations, first launch)
+            if (!err) err = cudaDeviceSynchronize() == cudaSuccess ? 0 : MSGPU_E_CUDA;
+            float ms = 0.0f;
+            if (!err) {
+                cudaEventRecord(e0, nullptr);
+                err = msgpu_job_run(J, nullptr);
+                cudaEventRecord(e1, nullptr);
+                if (!err && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            msgpu_job_destroy(J);
+            if (err) return err;
+            t = 1e-3 * ms;
+            if (best == 0.0 || t < best) {
+                best = t;
+                best_e = eng;
+                best_c = c;
+            }
+        }
+    return msgpu_tune_set(kind, precision, n, best_e, best_c);
 }
 
 static int run_batch(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,

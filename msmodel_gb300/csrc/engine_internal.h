@@ -25,7 +25,7 @@ struct EngineParams {
     int piv_stride;
     double* out;          // 2 * nitem
     int* status;          // nitem
-    unsigned* counter;
+    unsigned* counter;    // [0] work queue; [1] live items (queue positions >= it are past the end)
     int kind;             // 0 ln det / n, 1 dlogf, 2 amplitudes a = M^-1 phi
     double* amps;         // kind 2: a per item (2 * n_i doubles each) or nullptr
     const long long* amp_off;  // kind 2: offset (in complex elements) of item i in amps
@@ -38,6 +38,11 @@ void count_launches(int n);
 // Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
 // negative MSGPU_E* code on error.
 int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st);
+// Allocates the mixed engine's scratch for `grid` CTAs and matrices up to nmax
+// (mixed_run does so itself; called before a stream capture, which must not allocate).
+int mixed_prepare(int grid, int nmax);
+// Changes whenever the mixed engine's scratch is reallocated (captured graphs hold its address).
+unsigned long long mixed_generation();
 // kernels launched by the mixed engine for one run
 int mixed_launches();
 // per-phase SM cycles of the last mixed run made with MSGPU_STATS set:

@@ -108,4 +108,126 @@ __device__ __forceinline__ void pair_elements_df3(zc k, double r, bool want_deri
     }
 }
 
+// ---------------------------------------------------------------------------
+// All-FP32-pipe form of the d = 3 Green function, for the wavefunction grid
+// (pixels x atoms evaluations), where FP64 sqrt, division and reductions per
+// pair would keep the FP64 pipe the bound.  Only the coordinates are
+// converted from FP64, once per tile.
+//
+//   r      double-float sqrt: FP32 root plus one Newton correction
+//   phase  phi = Re k * r reduced modulo pi/16 (three-float split of pi/16,
+//          each product q * part exact by FMA), |y| <= pi/32; sin/cos of
+//          j pi/16 from a 32-entry table, sin/cos of y by Taylor series
+//          (next terms < 4e-17), combined by the addition theorem
+//   growth e^{-Im k * r} reduced modulo ln2/16, 2^{j/16} from a 16-entry
+//          table, e^t by Taylor series (|t| <= ln2/32, next term < 2e-18)
+// Relative accuracy about 2^-44 per element (|phi| * 2^-47 absolute in the
+// phase); values are FP32-range limited, so callers keep |Im k| r below 80.
+
+__device__ __forceinline__ df two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return df{p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ df df_sqrt(df a) {
+    if (!(a.h > 0.0f)) return df{0.0f, 0.0f};
+    const float s = __fsqrt_rn(a.h);
+    const df p = two_prod(s, s);
+    const float e = __fadd_rn(__fsub_rn(__fsub_rn(a.h, p.h), p.l), a.l);
+    return quick_two_sum(s, __fmul_rn(e, __fmul_rn(0.5f, __frcp_rn(s))));
+}
+
+__device__ __forceinline__ df df_recip(df b) {
+    const float q1 = __frcp_rn(b.h);
+    float r = __fmaf_rn(-b.h, q1, 1.0f);
+    r = __fmaf_rn(-b.l, q1, r);
+    return quick_two_sum(q1, __fmul_rn(r, q1));
+}
+
+struct Df3Tables {
+    float4 sc[32];  // {sin.h, sin.l, cos.h, cos.l} of j pi/16
+    float2 p2[16];  // 2^{j/16}
+};
+
+// fill by threads 0..31 of the block (FP64 sincospi / exp2 of exact arguments)
+__device__ __forceinline__ void df3_tables_init(Df3Tables& t) {
+    const int j = threadIdx.x;
+    if (j < 32) {
+        double s, c;
+        sincospi(j / 16.0, &s, &c);
+        const df ds = df_from_double(s), dc = df_from_double(c);
+        t.sc[j] = make_float4(ds.h, ds.l, dc.h, dc.l);
+    }
+    if (j < 16) {
+        const df p = df_from_double(exp2(j / 16.0));
+        t.p2[j] = make_float2(p.h, p.l);
+    }
+}
+
+// e^{i phi} for phi = kr * r
+__device__ __forceinline__ void df_cis(const Df3Tables& t, df phi, df& cs, df& sn) {
+    const float q = rintf(__fmul_rn(phi.h, 5.0929582f));  // 16 / pi
+    df y = df_sub(phi, two_prod(q, 0.19634955f));
+    y = df_sub(y, two_prod(q, -5.4639235e-09f));
+    y = quick_two_sum(y.h, __fmaf_rn(-q, -2.1439056e-16f, y.l));
+    const df nu = df_neg(df_mul(y, y));
+    df ps = df{2.7557319e-06f, 0.0f}, pc = df{2.4801588e-05f, 0.0f};  // 1/9!, 1/8!
+#pragma unroll
+    for (int k = 3; k >= 0; --k) {
+        ps = df_add(df_mul(ps, nu), invfact(2 * k + 1));
+        pc = df_add(df_mul(pc, nu), invfact(2 * k));
+    }
+    const df s = df_mul(ps, y), c = pc;
+    const float4 e = t.sc[((int)q) & 31];
+    const df S{e.x, e.y}, C{e.z, e.w};
+    sn = df_add(df_mul(S, c), df_mul(C, s));
+    cs = df_sub(df_mul(C, c), df_mul(S, s));
+}
+
+// e^{x}, |x| < 80
+__device__ __forceinline__ df df_exp_tab(const Df3Tables& t, df x) {
+    const float q = rintf(__fmul_rn(x.h, 23.08312f));  // 16 / ln 2
+    df y = df_sub(x, two_prod(q, 0.0433217f));
+    y = df_sub(y, two_prod(q, -1.1904089e-10f));
+    y = quick_two_sum(y.h, __fmaf_rn(-q, -5.48949e-18f, y.l));
+    df p = invfact(7);
+#pragma unroll
+    for (int k = 6; k >= 0; --k) p = df_add(df_mul(p, y), invfact(k));
+    const int qi = (int)q;
+    const float2 m = t.p2[qi & 15];
+    p = df_mul(p, df{m.x, m.y});
+    const int sh = qi >> 4;  // floor(q / 16)
+    return df{ldexpf(p.h, sh), ldexpf(p.l, sh)};
+}
+
+// M_ij = e^{ikr} / (4 pi r) and dM_ij = i e^{ikr} / (4 pi) of d = 3 from a
+// double-float r, entirely on the FP32 pipe (grow: Im k != 0)
+__device__ __forceinline__ void pair_elements_df3t(const Df3Tables& t, df kr, df ki, bool grow, df r,
+                                                   bool want_deriv, dfc& m, dfc& dm) {
+    df cs, sn;
+    df_cis(t, df_mul(kr, r), cs, sn);
+    const df e = grow ? df_exp_tab(t, df_neg(df_mul(ki, r))) : df{1.0f, 0.0f};
+    const df fourpi{12.566371f, -3.496911e-07f};
+    const df w = df_mul(e, df_recip(df_mul(fourpi, r)));
+    m = dfc{df_mul(w, cs), df_mul(w, sn)};
+    if (want_deriv) {
+        const df w2 = df_mul(e, df{0.07957747f, 3.2103191e-09f});  // 1 / (4 pi)
+        dm = dfc{df_neg(df_mul(w2, sn)), df_mul(w2, cs)};
+    }
+}
+
+// a * G(k, r) of d = 3, G = -e^{ikr} / (4 pi r), accumulated into acc
+__device__ __forceinline__ void df3_green_mac(const Df3Tables& t, df kr, df ki, bool grow, df r, dfc a, dfc& acc) {
+    df cs, sn;
+    df_cis(t, df_mul(kr, r), cs, sn);
+    const df fourpi{12.566371f, -3.496911e-07f};
+    df w = df_recip(df_mul(fourpi, r));
+    if (grow) w = df_mul(w, df_exp_tab(t, df_neg(df_mul(ki, r))));
+    // acc -= w * a * (cs + i sn)
+    const df vr = df_sub(df_mul(a.re, cs), df_mul(a.im, sn));
+    const df vi = df_add(df_mul(a.re, sn), df_mul(a.im, cs));
+    acc.re = df_sub(acc.re, df_mul(w, vr));
+    acc.im = df_sub(acc.im, df_mul(w, vi));
+}
+
 }  // namespace msg

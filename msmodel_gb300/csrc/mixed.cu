@@ -50,6 +50,10 @@ struct MixPanel {
     float4 T[NB][NB + 1];
     float4 T2[NB][NB + 1];
     float4 urow[NB];
+    // assembly of d = 3: sin/cos/2^x tables, coordinates of the tile's atoms as double-floats
+    Df3Tables tab;
+    float4 ci[NB], cj[NB];  // x.h x.l y.h y.l
+    float2 ciz[NB], cjz[NB];
 };
 struct MixGemm {
     uint8_t A[A_BAND];
@@ -68,6 +72,8 @@ struct MixSmem {
     zc diag[2];
     double red_v[NT / 32];
     int red_i[NT / 32];
+    float red_f[NT / 32];
+    float4 rcp;  // reciprocal of the current pivot (double-float complex)
     double red_s[3][NT / 32];
     int info, bcast_i, item;
     unsigned long long stat[PH_N];
@@ -359,73 +365,153 @@ __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __
 }
 
 // ---------------------------------------------------------------- double-float panel, TRSM, solves
-__device__ void df_panel(float4* __restrict__ A, int n, int j0, int jb, int* __restrict__ ipiv, MixSmem& s) {
+// arg max of v over the CTA (smallest index on ties), in FP32: the FP64 pipe
+// (1/64 of the FP32 rate on GB300) stays out of the panel's per-column steps
+__device__ __forceinline__ int block_argmaxf(float v, int i, MixSmem& s) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float v2 = __shfl_down_sync(FULL, v, off);
+        const int i2 = __shfl_down_sync(FULL, i, off);
+        if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+    }
+    if (lane == 0) { s.red_f[warp] = v; s.red_i[warp] = i; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float bv = s.red_f[0];
+        int bi = s.red_i[0];
+        for (int w = 1; w < NT / 32; w++) {
+            const float v2 = s.red_f[w];
+            const int i2 = s.red_i[w];
+            if (v2 > bv || (v2 == bv && i2 < bi)) { bv = v2; bi = i2; }
+        }
+        s.bcast_i = bi;
+    }
+    __syncthreads();
+    return s.bcast_i;
+}
+
+// Panel factorisation in double-float: LAPACK's getf2 pivoting (|Re|+|Im|,
+// first index on ties, full-panel row interchanges), organised in sub-panels
+// of SW columns.  Inside a sub-panel the rank-1 updates touch only its own
+// columns; the rest of the panel then takes one rank-SW update per sub-panel
+// (U rows by unit-lower substitution in shared memory).  The panel of a large
+// matrix does not stay in L2 across 304 resident CTAs, so this cuts its
+// memory traffic (the full-width rank-1 form re-reads and re-writes the whole
+// remaining panel once per column) by about 2.4x at the same arithmetic.
+// Not inlined: its registers are then allocated apart from the engine's
+// tensor-core epilogue, which holds the kernel at the 128-register cap.
+constexpr int SW = 4;
+
+__device__ __noinline__ void df_panel(float4* __restrict__ A, int n, int j0, int jb, int* __restrict__ ipiv, MixSmem& s) {
     const int tid = threadIdx.x;
     const int cend = j0 + jb;
-    double bv = -1.0;
+    float bv = -1.0f;
     int bi = n;
     for (int i = j0 + tid; i < n; i += NT) {
-        double v = dfc_abs1(dfc_load(A + i + (size_t)j0 * n));
+        const float v = dfc_abs1(dfc_load(A + i + (size_t)j0 * n));
         if (v > bv) { bv = v; bi = i; }
     }
-    for (int c = j0; c < cend; ++c) {
-        int p;
-        block_argmax(bv, bi, s, p);
-        if (p >= n) p = c;
-        const dfc piv = dfc_load(A + p + (size_t)c * n);
-        const bool nz = !dfc_is_zero(piv);
-        if (tid == 0) {
-            ipiv[c] = p;
-            if (!nz && s.info == 0) s.info = c + 1;
-        }
-        __syncthreads();  // every thread holds the pivot before row p is swapped away
-        if (nz && p != c && tid < jb) {
-            const size_t col = (size_t)(j0 + tid) * n;
-            float4 t = A[c + col];
-            A[c + col] = A[p + col];
-            A[p + col] = t;
-        }
-        __syncthreads();
-        if (tid < jb && j0 + tid > c) s.u.p.urow[tid] = A[c + (size_t)(j0 + tid) * n];
-        __syncthreads();
-        bv = -1.0;
-        bi = n;
-        if (nz) {
-            // reciprocal of the pivot in FP64, once per column
-            const zc pz = mk(df_to_double(piv.re), df_to_double(piv.im));
-            const zc rz = 1.0 / pz;
-            const dfc r = dfc{df_from_double(rz.re), df_from_double(rz.im)};
-            for (int i = c + 1 + tid; i < n; i += NT) {
-                float4* pc = A + i + (size_t)c * n;
-                const dfc l = dfc_mul(dfc_load(pc), r);
-                dfc_store(pc, l);
-                if (c + 1 < cend) {
-                    float4* q1 = A + i + (size_t)(c + 1) * n;
-                    const dfc a = dfc_fms(dfc_load(q1), l, dfc_load(&s.u.p.urow[c + 1 - j0]));
-                    dfc_store(q1, a);
-                    double v = dfc_abs1(a);
-                    if (v > bv) { bv = v; bi = i; }
-                    int cc = c + 2;
-                    for (; cc + 4 <= cend; cc += 4) {  // four independent loads in flight
-                        float4 v[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) v[u] = A[i + (size_t)(cc + u) * n];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            dfc_store(A + i + (size_t)(cc + u) * n,
-                                      dfc_fms(dfc{df{v[u].x, v[u].y}, df{v[u].z, v[u].w}}, l,
-                                              dfc_load(&s.u.p.urow[cc + u - j0])));
+    for (int c0 = j0; c0 < cend; c0 += SW) {
+        const int sw = min(c0 + SW, cend);  // sub-panel columns [c0, sw)
+        for (int c = c0; c < sw; ++c) {
+            int p = block_argmaxf(bv, bi, s);
+            if (p >= n) p = c;
+            const dfc piv = dfc_load(A + p + (size_t)c * n);
+            const bool nz = !dfc_is_zero(piv);
+            if (tid == 0) {
+                ipiv[c] = p;
+                if (!nz && s.info == 0) s.info = c + 1;
+                if (nz) {  // the pivot's reciprocal, once per column, in FP64
+                    const zc rz = 1.0 / mk(df_to_double(piv.re), df_to_double(piv.im));
+                    const df a = df_from_double(rz.re), b = df_from_double(rz.im);
+                    s.rcp = make_float4(a.h, a.l, b.h, b.l);
+                }
+            }
+            __syncthreads();  // every thread holds the pivot before row p is swapped away
+            if (nz && p != c && tid < jb) {
+                const size_t col = (size_t)(j0 + tid) * n;
+                float4 t = A[c + col];
+                A[c + col] = A[p + col];
+                A[p + col] = t;
+            }
+            __syncthreads();
+            if (tid < jb && j0 + tid > c && j0 + tid < sw) s.u.p.urow[tid] = A[c + (size_t)(j0 + tid) * n];
+            __syncthreads();
+            bv = -1.0f;
+            bi = n;
+            if (nz) {
+                const dfc r = dfc_load(&s.rcp);
+                for (int i = c + 1 + tid; i < n; i += NT) {
+                    float4* pc = A + i + (size_t)c * n;
+                    const dfc l = dfc_mul(dfc_load(pc), r);
+                    dfc_store(pc, l);
+                    if (c + 1 < sw) {
+                        float4* q1 = A + i + (size_t)(c + 1) * n;
+                        const dfc a = dfc_fms(dfc_load(q1), l, dfc_load(&s.u.p.urow[c + 1 - j0]));
+                        dfc_store(q1, a);
+                        const float v = dfc_abs1(a);
+                        if (v > bv) { bv = v; bi = i; }
+                        for (int cc = c + 2; cc < sw; ++cc) {
+                            float4* qp = A + i + (size_t)cc * n;
+                            dfc_store(qp, dfc_fms(dfc_load(qp), l, dfc_load(&s.u.p.urow[cc - j0])));
+                        }
                     }
-                    for (; cc < cend; ++cc) {
-                        float4* qp = A + i + (size_t)cc * n;
-                        dfc_store(qp, dfc_fms(dfc_load(qp), l, dfc_load(&s.u.p.urow[cc - j0])));
+                }
+            } else if (c + 1 < sw) {
+                for (int i = c + 1 + tid; i < n; i += NT) {
+                    const float v = dfc_abs1(dfc_load(A + i + (size_t)(c + 1) * n));
+                    if (v > bv) { bv = v; bi = i; }
+                }
+            }
+        }
+        if (sw < cend) {
+            const int cw = sw - c0, rem = cend - sw;
+            __syncthreads();  // the sub-panel's last column is complete
+            // L11 (unit lower, cw x cw) into shared memory
+            if (tid < cw * cw) {
+                const int r = tid / cw, q = tid % cw;
+                if (q < r) s.u.p.T2[r][q] = A[c0 + r + (size_t)(c0 + q) * n];
+            }
+            __syncthreads();
+            // U rows of the sub-panel for columns [sw, cend): u_r = a_r - sum_{q<r} L_rq u_q
+            if (tid < rem) {
+                const size_t col = (size_t)(sw + tid) * n;
+                dfc u[SW];
+#pragma unroll
+                for (int r = 0; r < SW; ++r) {
+                    if (r < cw) {
+                        dfc a = dfc_load(A + c0 + r + col);
+#pragma unroll
+                        for (int q = 0; q < r; ++q) a = dfc_fms(a, dfc_load(&s.u.p.T2[r][q]), u[q]);
+                        u[r] = a;
+                        dfc_store(A + c0 + r + col, a);
+                        dfc_store(&s.u.p.T[r][tid], a);
                     }
                 }
             }
-        } else if (c + 1 < cend) {
-            for (int i = c + 1 + tid; i < n; i += NT) {
-                double v = dfc_abs1(dfc_load(A + i + (size_t)(c + 1) * n));
-                if (v > bv) { bv = v; bi = i; }
+            __syncthreads();
+            // rank-cw update of rows >= sw; argmax of column sw on the way
+            bv = -1.0f;
+            bi = n;
+            for (int i = sw + tid; i < n; i += NT) {
+                dfc l[SW];
+#pragma unroll
+                for (int q = 0; q < SW; ++q)
+                    if (q < cw) l[q] = dfc_load(A + i + (size_t)(c0 + q) * n);
+                for (int t = 0; t < rem; ++t) {
+                    float4* qp = A + i + (size_t)(sw + t) * n;
+                    dfc a = dfc_load(qp);
+#pragma unroll
+                    for (int q = 0; q < SW; ++q)
+                        if (q < cw) a = dfc_fms(a, l[q], dfc_load(&s.u.p.T[q][t]));
+                    dfc_store(qp, a);
+                    if (t == 0) {
+                        const float v = dfc_abs1(a);
+                        if (v > bv) { bv = v; bi = i; }
+                    }
+                }
             }
         }
     }
@@ -588,6 +674,13 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
     }
     __syncthreads();
     const zc dg0 = s.diag[0], dg1 = s.diag[1];
+    const bool d3 = d == 3;
+    const df kr = df_from_double(k.re), ki = df_from_double(k.im);
+    const bool grow = k.im != 0.0;
+    if (d3) {
+        df3_tables_init(s.u.p.tab);
+        __syncthreads();
+    }
     float mx = 0.0f;
     auto cvt = [](zc v) {
         df a = df_from_double(v.re), b = df_from_double(v.im);
@@ -596,16 +689,42 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
     const int nt = (n + 31) / 32;
     for (int J = 0; J < nt; ++J) {
         for (int I = 0; I <= J; ++I) {
+            if (d3) {
+                // the tile's atoms as double-floats: rows I*32.., columns J*32..
+                if (tid < 64) {
+                    const int a = (tid < 32 ? I : J) * 32 + (tid & 31);
+                    df x{0.0f, 0.0f}, y{0.0f, 0.0f}, z{0.0f, 0.0f};
+                    if (a < n) {
+                        x = df_from_double(pos[3 * a]);
+                        y = df_from_double(pos[3 * a + 1]);
+                        z = df_from_double(pos[3 * a + 2]);
+                    }
+                    if (tid < 32) {
+                        s.u.p.ci[tid] = make_float4(x.h, x.l, y.h, y.l);
+                        s.u.p.ciz[tid] = make_float2(z.h, z.l);
+                    } else {
+                        s.u.p.cj[tid - 32] = make_float4(x.h, x.l, y.h, y.l);
+                        s.u.p.cjz[tid - 32] = make_float2(z.h, z.l);
+                    }
+                }
+                __syncthreads();
+            }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
                 const int i = I * 32 + ii, j = J * 32 + jj;
                 if (i < n && j < n && i <= j) {
                     float4 fm, fd = make_float4(0, 0, 0, 0);
-                    if (i < j && d == 3) {
-                        // transcendentals on the FP32 pipe in double-float (green_df.cuh)
+                    if (i < j && d3) {
+                        // the whole element on the FP32 pipe in double-float (green_df.cuh)
+                        const float4 pa = s.u.p.ci[ii], pb = s.u.p.cj[jj];
+                        const float2 za = s.u.p.ciz[ii], zb = s.u.p.cjz[jj];
+                        const df ex = df_sub(df{pa.x, pa.y}, df{pb.x, pb.y});
+                        const df ey = df_sub(df{pa.z, pa.w}, df{pb.z, pb.w});
+                        const df ez = df_sub(df{za.x, za.y}, df{zb.x, zb.y});
+                        const df r = df_sqrt(df_add(df_add(df_mul(ex, ex), df_mul(ey, ey)), df_mul(ez, ez)));
                         dfc a, b;
-                        pair_elements_df3(k, atom_distance(d, pos, i, j), B != nullptr, a, b);
+                        pair_elements_df3t(s.u.p.tab, kr, ki, grow, r, B != nullptr, a, b);
                         fm = make_float4(a.re.h, a.re.l, a.im.h, a.im.l);
                         if (B) fd = make_float4(b.re.h, b.re.l, b.im.h, b.im.l);
                     } else {
@@ -831,7 +950,8 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
     bool alive = true;
     while (alive) {
         if (tid == 0) {
-            s.item = (int)atomicAdd(P.counter, 1u);
+            const unsigned q = atomicAdd(P.counter, 1u);
+            s.item = q < P.counter[1] ? (int)q : P.nitem;
             s.info = 0;
         }
         __syncthreads();
@@ -910,8 +1030,10 @@ int g_launches_last = 0;
 
 static size_t mixed_smem() { return sizeof(MixSmem) + 1024; }
 
-int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
-    std::lock_guard<std::mutex> lk(g_mx);
+unsigned long long g_mix_gen = 1;
+
+// scratch layout for `grid` CTAs and matrices up to nmax; allocates when it grows
+static int prepare_locked(int grid, int nmax, MixScratch& X) {
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_engine_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mixed_smem()) !=
@@ -919,10 +1041,6 @@ int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
             return MSGPU_E_CUDA;
         attr = true;
     }
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_engine_mixed, NT, mixed_smem()) != cudaSuccess || occ < 1)
-        return MSGPU_E_CUDA;
-    MixScratch X;
     const int nbA = (nmax + MT_M - 1) / MT_M, nbB = (nmax + MT_N - 1) / MT_N;
     X.a_stride = (size_t)nbA * A_BAND;
     X.b_stride = (size_t)nbB * B_BAND;
@@ -932,21 +1050,43 @@ int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
         if (g_img) cudaFree(g_img);
         g_img = nullptr;
         g_img_bytes = 0;
+        ++g_mix_gen;
         if (cudaMalloc(&g_img, need) != cudaSuccess) return MSGPU_E_CUDA;
         g_img_bytes = need;
     }
-    if (!g_err && cudaMalloc(&g_err, sizeof(int)) != cudaSuccess) return MSGPU_E_CUDA;
+    if (!g_err) {
+        ++g_mix_gen;
+        if (cudaMalloc(&g_err, sizeof(int)) != cudaSuccess) return MSGPU_E_CUDA;
+    }
+    if (getenv("MSGPU_STATS") && !g_stats) {
+        ++g_mix_gen;
+        if (cudaMalloc(&g_stats, sizeof(unsigned long long) * PH_N) != cudaSuccess) return MSGPU_E_CUDA;
+    }
     X.imgA = g_img;
     X.imgB = g_img + (size_t)grid * X.a_stride;
     X.ea = reinterpret_cast<int*>(X.imgB + (size_t)grid * X.b_stride);
     X.eb = X.ea + (size_t)grid * X.e_stride;
     X.err = g_err;
-    X.stats = nullptr;
-    if (getenv("MSGPU_STATS")) {
-        if (!g_stats && cudaMalloc(&g_stats, sizeof(unsigned long long) * PH_N) != cudaSuccess) return MSGPU_E_CUDA;
-        cudaMemsetAsync(g_stats, 0, sizeof(unsigned long long) * PH_N, st);
-        X.stats = g_stats;
-    }
+    X.stats = getenv("MSGPU_STATS") ? g_stats : nullptr;
+    return 0;
+}
+
+int mixed_prepare(int grid, int nmax) {
+    std::lock_guard<std::mutex> lk(g_mx);
+    MixScratch X;
+    return prepare_locked(grid, nmax, X);
+}
+
+unsigned long long mixed_generation() {
+    std::lock_guard<std::mutex> lk(g_mx);
+    return g_mix_gen;
+}
+
+int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_mx);
+    MixScratch X;
+    if (int e = prepare_locked(grid, nmax, X)) return e;
+    if (X.stats) cudaMemsetAsync(X.stats, 0, sizeof(unsigned long long) * PH_N, st);
     if (cudaMemsetAsync(P.counter, 0, sizeof(unsigned), st) != cudaSuccess) return MSGPU_E_CUDA;
     k_engine_mixed<<<grid, NT, mixed_smem(), st>>>(P, X);
     g_launches_last = 1;

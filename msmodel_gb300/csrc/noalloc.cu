@@ -40,7 +40,8 @@ __global__ void k_noalloc_setup(MedDev* md, MedDev v, unsigned* counter, int* it
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         *md = v;
-        *counter = 0u;
+        counter[0] = 0u;
+        counter[1] = (unsigned)nitem;  // live items of the work queue
     }
     for (; i < nitem; i += gridDim.x * blockDim.x) {
         item_med[i] = 0;

@@ -6,124 +6,228 @@
 // src/core/wave_function_util.c:76-81).  Averaged over media (seeds): the
 // real part and |psi|^2, as the reference accumulates them.
 //
-// One thread per pixel; atoms stream through shared memory in tiles of 256
-// (x, y, squared remaining coordinates, a).  FP64 throughout: pixels x atoms
-// Green evaluations, bound by the FP64 pipe.
+// Several wave numbers at once: every (medium, k) solve goes into one
+// amplitude job (one persistent engine launch), then one grid launch per
+// medium covers every k (blockIdx.y), accumulating into per-k planes.
+//
+// One thread per pixel; atoms stream through shared memory in tiles of 256.
+//   FP64 kernel : the reference's arithmetic, bound by the FP64 pipe.
+//   DF kernel   : d = 3 only, the Green function in double-float arithmetic
+//                 on the FP32 pipe (green_df.cuh), used by the mixed precision
+//                 when |Im k| * r stays below 80 over the grid.
 #include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
 #include <vector>
 #include "msgpu.h"
 #include "green.cuh"
+#include "green_df.cuh"
 #include "engine_internal.h"
 
 namespace msg {
 
 constexpr int PT = 256;
 
-__global__ void __launch_bounds__(PT) k_psi_grid(int d, int n, const double* __restrict__ pos,
-                                                 const double* __restrict__ amp, double kre, double kim, int nx,
-                                                 int ny, double xmin, double dx, double ymax, double dy,
-                                                 double* __restrict__ fun, double* __restrict__ den,
-                                                 double* __restrict__ psi) {
+struct GridArgs {
+    int d, n, nx, ny;
+    const double* pos;
+    const double* amp;  // [nk][n] complex
+    const double* ks;   // [nk] complex
+    double xmin, dx, ymax, dy;
+    double* fun;  // [nk][nx*ny]
+    double* den;
+    double* psi;  // [nk][nx*ny] complex, or null
+};
+
+__device__ __forceinline__ void finish_pixel(const GridArgs& A, int kk, int l, double px, zc acc) {
+    const size_t o = (size_t)kk * A.nx * A.ny + l;
+    const zc k = mk(A.ks[2 * kk], A.ks[2 * kk + 1]);
+    const zc v = acc + zexp(mk(0.0, 1.0) * k * px);
+    A.fun[o] += v.re;
+    A.den[o] += v.re * v.re + v.im * v.im;
+    if (A.psi) {
+        A.psi[2 * o] = v.re;
+        A.psi[2 * o + 1] = v.im;
+    }
+}
+
+__global__ void __launch_bounds__(PT) k_psi_grid(GridArgs A) {
     __shared__ double sx[PT], sy[PT], sr[PT], sar[PT], sai[PT];
+    const int kk = blockIdx.y;
     const int l = blockIdx.x * PT + threadIdx.x;
-    const bool live = l < nx * ny;
-    const double px = xmin + (l % nx) * dx, py = ymax - (l / nx) * dy;
-    const zc k = mk(kre, kim);
+    const bool live = l < A.nx * A.ny;
+    const double px = A.xmin + (l % A.nx) * A.dx, py = A.ymax - (l / A.nx) * A.dy;
+    const zc k = mk(A.ks[2 * kk], A.ks[2 * kk + 1]);
+    const double* amp = A.amp + 2 * (size_t)kk * A.n;
     zc acc = mk(0.0);
-    for (int t0 = 0; t0 < n; t0 += PT) {
+    for (int t0 = 0; t0 < A.n; t0 += PT) {
         const int i = t0 + threadIdx.x;
-        if (i < n) {
-            const double* p = pos + (size_t)i * d;
+        if (i < A.n) {
+            const double* p = A.pos + (size_t)i * A.d;
             sx[threadIdx.x] = p[0];
-            sy[threadIdx.x] = d > 1 ? p[1] : 0.0;
+            sy[threadIdx.x] = A.d > 1 ? p[1] : 0.0;
             double rest = 0.0;
-            for (int c = 2; c < d; ++c) rest += p[c] * p[c];
+            for (int c = 2; c < A.d; ++c) rest += p[c] * p[c];
             sr[threadIdx.x] = rest;
             sar[threadIdx.x] = amp[2 * i];
             sai[threadIdx.x] = amp[2 * i + 1];
         }
         __syncthreads();
-        const int cnt = min(PT, n - t0);
+        const int cnt = min(PT, A.n - t0);
         if (live) {
             for (int j = 0; j < cnt; ++j) {
                 const double ex = sx[j] - px, ey = sy[j] - py;
                 const double r = sqrt(ex * ex + ey * ey + sr[j]);
-                const zc g = free_green(d, k, r);
-                acc += mk(sar[j], sai[j]) * g;
+                acc += mk(sar[j], sai[j]) * free_green(A.d, k, r);
             }
         }
         __syncthreads();
     }
-    if (!live) return;
-    const zc v = acc + zexp(mk(0.0, 1.0) * k * px);
-    fun[l] += v.re;
-    den[l] += v.re * v.re + v.im * v.im;
-    if (psi) {
-        psi[2 * l] = v.re;
-        psi[2 * l + 1] = v.im;
+    if (live) finish_pixel(A, kk, l, px, acc);
+}
+
+__global__ void __launch_bounds__(PT) k_psi_grid_df3(GridArgs A) {
+    __shared__ Df3Tables tab;
+    __shared__ float4 sxy[PT];  // x.h x.l y.h y.l
+    __shared__ float2 sz[PT];   // z^2 (d = 3)
+    __shared__ float4 sa[PT];   // a as double-float complex
+    df3_tables_init(tab);
+    const int kk = blockIdx.y;
+    const int l = blockIdx.x * PT + threadIdx.x;
+    const bool live = l < A.nx * A.ny;
+    const double pxd = A.xmin + (l % A.nx) * A.dx, pyd = A.ymax - (l / A.nx) * A.dy;
+    const df px = df_from_double(pxd), py = df_from_double(pyd);
+    const df kr = df_from_double(A.ks[2 * kk]), ki = df_from_double(A.ks[2 * kk + 1]);
+    const bool grow = A.ks[2 * kk + 1] != 0.0;
+    const double* amp = A.amp + 2 * (size_t)kk * A.n;
+    dfc acc{df{0.0f, 0.0f}, df{0.0f, 0.0f}};
+    for (int t0 = 0; t0 < A.n; t0 += PT) {
+        const int i = t0 + threadIdx.x;
+        if (i < A.n) {
+            const double* p = A.pos + (size_t)i * 3;
+            const df x = df_from_double(p[0]), y = df_from_double(p[1]), z2 = df_from_double(p[2] * p[2]);
+            sxy[threadIdx.x] = make_float4(x.h, x.l, y.h, y.l);
+            sz[threadIdx.x] = make_float2(z2.h, z2.l);
+            const df ar = df_from_double(amp[2 * i]), ai = df_from_double(amp[2 * i + 1]);
+            sa[threadIdx.x] = make_float4(ar.h, ar.l, ai.h, ai.l);
+        }
+        __syncthreads();
+        const int cnt = min(PT, A.n - t0);
+        if (live) {
+            for (int j = 0; j < cnt; ++j) {
+                const float4 q = sxy[j];
+                const float2 z = sz[j];
+                const df ex = df_sub(df{q.x, q.y}, px), ey = df_sub(df{q.z, q.w}, py);
+                const df r2 = df_add(df_add(df_mul(ex, ex), df_mul(ey, ey)), df{z.x, z.y});
+                const float4 a = sa[j];
+                df3_green_mac(tab, kr, ki, grow, df_sqrt(r2), dfc{df{a.x, a.y}, df{a.z, a.w}}, acc);
+            }
+        }
+        __syncthreads();
     }
+    if (live) finish_pixel(A, kk, l, pxd, mk(df_to_double(acc.re), df_to_double(acc.im)));
 }
 
 }  // namespace msg
 
-// Seed-averaged wavefunction of run_wave_function_omp: media[m] are the
-// realisations (all of the same n, d), k the incident wave number.
-// function/density: nx*ny doubles (averaged Re psi and |psi|^2); psi (may be
-// NULL): complex psi of media[0]; amps (may be NULL): a of every medium.
-extern "C" int msgpu_wave_function(int nmed, const msgpu_medium* media, const double* k, int nx, int ny,
-                                   const double* dom, double* function, double* density, double* psi,
-                                   double* amps, int precision) {
+extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, int nk, const double* ks, int nx,
+                                         int ny, const double* dom, double* function, double* density, double* psi,
+                                         double* amps, int precision) {
     using namespace msg;
-    if (nmed < 1 || !media || !k || nx < 2 || ny < 2 || !dom || !function || !density) return MSGPU_E_ARG;
+    if (nmed < 1 || !media || nk < 1 || !ks || nx < 2 || ny < 2 || !dom || !function || !density) return MSGPU_E_ARG;
     const int n = media[0].n, d = media[0].d;
     for (int m = 0; m < nmed; ++m)
-        if (media[m].n != n || media[m].d != d) return MSGPU_E_ARG;
-    std::vector<double> ks(2 * (size_t)nmed), sig(2 * (size_t)nmed), a(2 * (size_t)nmed * n);
-    std::vector<int> im(nmed), st(nmed);
-    for (int m = 0; m < nmed; ++m) {
-        ks[2 * m] = k[0];
-        ks[2 * m + 1] = k[1];
-        im[m] = m;
-    }
-    int e = msgpu_amplitude_batch(nmed, media, nmed, im.data(), ks.data(), sig.data(), a.data(), st.data(), precision);
+        if (media[m].n != n || media[m].d != d || !media[m].pos) return MSGPU_E_ARG;
+    const size_t np = (size_t)nx * ny;
+    if (np > (size_t)1 << 31 || (size_t)nk > 65535) return MSGPU_E_SIZE;
+    // every (medium, k) solve in one job: item m * nk + kk
+    const int nitem = nmed * nk;
+    std::vector<double> iks(2 * (size_t)nitem), sig(2 * (size_t)nitem), a(2 * (size_t)nitem * n);
+    std::vector<int> im(nitem), st(nitem);
+    for (int m = 0; m < nmed; ++m)
+        for (int kk = 0; kk < nk; ++kk) {
+            const int it = m * nk + kk;
+            iks[2 * it] = ks[2 * kk];
+            iks[2 * it + 1] = ks[2 * kk + 1];
+            im[it] = m;
+        }
+    int e = msgpu_amplitude_batch(nmed, media, nitem, im.data(), iks.data(), sig.data(), a.data(), st.data(),
+                                  precision);
     if (e) return e;
     if (amps) std::copy(a.begin(), a.end(), amps);
-    const size_t np = (size_t)nx * ny;
-    double *dpos = nullptr, *damp = nullptr, *dfun = nullptr, *dden = nullptr, *dpsi = nullptr;
+    // the double-float Green function keeps values in FP32 range: |Im k| * r < 80
+    double rmax = 0.0, kimax = 0.0;
+    for (int kk = 0; kk < nk; ++kk) kimax = std::max(kimax, std::fabs(ks[2 * kk + 1]));
+    if (d == 3 && precision == MSGPU_MIXED) {
+        double lo[3] = {dom[0], dom[2], 0.0}, hi[3] = {dom[1], dom[3], 0.0};
+        for (int m = 0; m < nmed; ++m)
+            for (int i = 0; i < n; ++i)
+                for (int c = 0; c < 3; ++c) {
+                    lo[c] = std::min(lo[c], media[m].pos[3 * i + c]);
+                    hi[c] = std::max(hi[c], media[m].pos[3 * i + c]);
+                }
+        rmax = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                         (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    }
+    const bool use_df = d == 3 && precision == MSGPU_MIXED && kimax * rmax < 80.0;
+    double *dpos = nullptr, *damp = nullptr, *dks = nullptr, *dfun = nullptr, *dden = nullptr, *dpsi = nullptr;
     auto cleanup = [&]() {
-        cudaFree(dpos); cudaFree(damp); cudaFree(dfun); cudaFree(dden); cudaFree(dpsi);
+        cudaFree(dpos); cudaFree(damp); cudaFree(dks); cudaFree(dfun); cudaFree(dden); cudaFree(dpsi);
     };
-    if (cudaMalloc(&dpos, sizeof(double) * (size_t)n * d) || cudaMalloc(&damp, sizeof(double) * 2 * (size_t)n) ||
-        cudaMalloc(&dfun, sizeof(double) * np) || cudaMalloc(&dden, sizeof(double) * np) ||
-        (psi && cudaMalloc(&dpsi, sizeof(double) * 2 * np))) {
+    const size_t plane = np * nk;
+    if (cudaMalloc(&dpos, sizeof(double) * (size_t)n * d) || cudaMalloc(&damp, sizeof(double) * 2 * (size_t)nk * n) ||
+        cudaMalloc(&dks, sizeof(double) * 2 * nk) || cudaMalloc(&dfun, sizeof(double) * plane) ||
+        cudaMalloc(&dden, sizeof(double) * plane) || (psi && cudaMalloc(&dpsi, sizeof(double) * 2 * plane))) {
         cleanup();
         return MSGPU_E_CUDA;
     }
-    cudaMemset(dfun, 0, sizeof(double) * np);
-    cudaMemset(dden, 0, sizeof(double) * np);
-    const double dx = (dom[1] - dom[0]) / (nx - 1), dy = (dom[3] - dom[2]) / (ny - 1);
-    const unsigned blocks = (unsigned)((np + PT - 1) / PT);
+    cudaMemset(dfun, 0, sizeof(double) * plane);
+    cudaMemset(dden, 0, sizeof(double) * plane);
+    cudaMemcpy(dks, ks, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice);
+    GridArgs A;
+    A.d = d;
+    A.n = n;
+    A.nx = nx;
+    A.ny = ny;
+    A.pos = dpos;
+    A.amp = damp;
+    A.ks = dks;
+    A.xmin = dom[0];
+    A.dx = (dom[1] - dom[0]) / (nx - 1);
+    A.ymax = dom[3];
+    A.dy = (dom[3] - dom[2]) / (ny - 1);
+    A.fun = dfun;
+    A.den = dden;
+    const dim3 grid((unsigned)((np + PT - 1) / PT), (unsigned)nk);
     for (int m = 0; m < nmed; ++m) {
         cudaMemcpy(dpos, media[m].pos, sizeof(double) * (size_t)n * d, cudaMemcpyHostToDevice);
-        cudaMemcpy(damp, a.data() + 2 * (size_t)m * n, sizeof(double) * 2 * (size_t)n, cudaMemcpyHostToDevice);
-        k_psi_grid<<<blocks, PT>>>(d, n, dpos, damp, k[0], k[1], nx, ny, dom[0], dx, dom[3], dy, dfun, dden,
-                                   m == 0 ? dpsi : nullptr);
+        cudaMemcpy(damp, a.data() + 2 * (size_t)m * nk * n, sizeof(double) * 2 * (size_t)nk * n,
+                   cudaMemcpyHostToDevice);
+        A.psi = m == 0 ? dpsi : nullptr;
+        if (use_df) k_psi_grid_df3<<<grid, PT>>>(A);
+        else k_psi_grid<<<grid, PT>>>(A);
         count_launches(1);
         if (cudaGetLastError() != cudaSuccess) {
             cleanup();
             return MSGPU_E_CUDA;
         }
     }
-    std::vector<double> hf(np), hd(np);
-    cudaError_t ce = cudaMemcpy(hf.data(), dfun, sizeof(double) * np, cudaMemcpyDeviceToHost);
-    if (ce == cudaSuccess) ce = cudaMemcpy(hd.data(), dden, sizeof(double) * np, cudaMemcpyDeviceToHost);
-    if (ce == cudaSuccess && psi) ce = cudaMemcpy(psi, dpsi, sizeof(double) * 2 * np, cudaMemcpyDeviceToHost);
+    cudaError_t ce = cudaMemcpy(function, dfun, sizeof(double) * plane, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(density, dden, sizeof(double) * plane, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && psi) ce = cudaMemcpy(psi, dpsi, sizeof(double) * 2 * plane, cudaMemcpyDeviceToHost);
     cleanup();
     if (ce != cudaSuccess) return MSGPU_E_CUDA;
     // divide_wfun (wave_function_util.c:86): average over the realisations
-    for (size_t l = 0; l < np; ++l) {
-        function[l] = hf[l] / nmed;
-        density[l] = hd[l] / nmed;
+    for (size_t l = 0; l < plane; ++l) {
+        function[l] /= nmed;
+        density[l] /= nmed;
     }
     return 0;
+}
+
+// Seed-averaged wavefunction of run_wave_function_omp at one wave number k.
+extern "C" int msgpu_wave_function(int nmed, const msgpu_medium* media, const double* k, int nx, int ny,
+                                   const double* dom, double* function, double* density, double* psi,
+                                   double* amps, int precision) {
+    return msgpu_wave_function_batch(nmed, media, 1, k, nx, ny, dom, function, density, psi, amps, precision);
 }

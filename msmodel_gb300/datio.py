@@ -1,0 +1,87 @@
+"""Output files in the reference's ".dat" format, so that results computed here
+can be plotted and re-read by the reference's own tools.
+
+The reference appends INI-like sections to one output file; each writer here
+appends the section it names with the same keys, order and number formats:
+
+  [medium]           save_medium           src/core/medium_util.c:420-429
+                     (model line: save_scmodel, scattering_model_util.c:174-181)
+  [kplane]           save_complexmap       src/core/complex_map_util.c:236-249
+                     (color line: save_colorrule, color_rule_util.c:276-282)
+  [kcut]             save_complexcut       src/core/complex_cut_util.c:106-117
+  [random_function]  save_random_function  src/core/random_function_util.c:178-193
+  data= line         save_cdata            src/core/complex_data_util.c:21-28
+
+`parse_cdata` reads a data= line back (parse_complex_data,
+src/core/complex_vector_util.c:215-231).  Numbers go through C-style printf
+conversions (%g, %.16g, %+.16g), which Python's % operator reproduces.
+"""
+import numpy as np
+
+__all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
+           "save_random_function"]
+
+MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
+SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
+
+
+def format_cdata(data):
+    """The data= line of save_cdata: every value as "%.16lg%+.16lgi " then a newline."""
+    z = np.asarray(data, dtype=np.complex128).reshape(-1)
+    return "data=" + "".join("%.16g%+.16gi " % (v.real, v.imag) for v in z) + "\n"
+
+
+def parse_cdata(line, n=None):
+    """Complex values of a data= line (or of the text after "data=")."""
+    text = line.split("=", 1)[1] if line.startswith("data=") else line
+    out = []
+    for tok in text.split():
+        if not tok.endswith("i"):
+            raise ValueError(f"data corruption at {tok[:20]!r}")
+        body = tok[:-1]
+        # the imaginary part starts at the last sign that is not an exponent sign
+        cut = max(j for j in range(1, len(body)) if body[j] in "+-" and body[j - 1] not in "eE")
+        out.append(complex(float(body[:cut]), float(body[cut:])))
+        if n is not None and len(out) == n:
+            break
+    return np.asarray(out, dtype=np.complex128)
+
+
+def _append(fname, text):
+    with open(fname, "a") as f:
+        f.write(text)
+
+
+def save_medium(fname, d, n, model="maximum", params=(), shape="ball", ratio=1.0):
+    name = model if isinstance(model, str) else MODEL_NAMES[model]
+    shp = shape if isinstance(shape, str) else SHAPE_NAMES[shape]
+    line = "model=" + name + "".join(" %.16g" % p for p in params)
+    _append(fname, "[medium]\ndimension=%d\nnatom=%d\n%s\nshape=%s\nratio=%g\n\n" % (d, n, line, shp, ratio))
+
+
+def save_complexmap(fname, data, nx, ny, xrange, yrange, title="", realtime=0.0, nseed=1,
+                    color=("magma", "seq", 3.0, False)):
+    """A [kplane] section; data in get_arg_cmap order (row-major from the top row)."""
+    cname, ctype, ctr, rev = color
+    text = ("[kplane]\ntitle=%s\nrealtime=%g\nnseed=%d\nxsample=%d\nysample=%d\nxrange=%g:%g\nyrange=%g:%g\n"
+            % (title, realtime, nseed, nx, ny, xrange[0], xrange[1], yrange[0], yrange[1]))
+    text += "color=%s %s %g%s\n" % (cname, ctype, ctr, " rev" if rev else "")
+    _append(fname, text + format_cdata(data) + "\n")
+
+
+def save_complexcut(fname, data, ns, kmin, kmax, title="", realtime=0.0, nseed=1):
+    """A [kcut] section; data in get_arg_ccut order (3 (ns+2) values)."""
+    kmin, kmax = complex(kmin), complex(kmax)
+    text = ("[kcut]\ntitle=%s\nrealtime=%g\nnseed=%d\nsample=%d\nkmin=%.12g%+.12gi\nkmax=%.12g%+.12gi\n"
+            % (title, realtime, nseed, ns, kmin.real, kmin.imag, kmax.real, kmax.imag))
+    _append(fname, text + format_cdata(data) + "\n")
+
+
+def save_random_function(fname, kind, data, xmin, xmax, title="", realtime=0.0):
+    """A [random_function] section; data[nbin, nseed] (bin-major, as computed)."""
+    data = np.asarray(data, dtype=np.float64)
+    nbin, nseed = data.shape
+    text = ("[random_function]\ntitle=%s\ntype=%s\nnseed=%d\nnbin=%d\nxmin=%.16g\nxmax=%.16g\nrealtime=%.16g\n"
+            % (title, kind, nseed, nbin, xmin, xmax, realtime))
+    text += "data=" + "".join("%.16g " % v for v in data.reshape(-1)) + "\n\n"
+    _append(fname, text)

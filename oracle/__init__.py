@@ -237,6 +237,9 @@ class Reference:
         L.ref_total_cross_section.restype = C.c_double
         L.ref_aberth.argtypes = med + [_dp, C.c_int, _dp, C.c_int, C.c_int, C.c_double]
         L.ref_wavefunction.argtypes = med + [_dp, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.ref_save_cdata.argtypes = [C.c_int, _dp, C.c_char_p]
+        L.ref_parse_cdata.argtypes = [C.c_int, C.c_char_p, _dp]
+        L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
 
     @staticmethod
     def _med(d, n, model, params, shape, ratio, seed):
@@ -283,6 +286,22 @@ class Reference:
 
     def total_cross_section(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
         return self.L.ref_total_cross_section(*self._med(d, n, model, params, shape, ratio, seed), float(k))
+
+    def save_cdata(self, values, fname):
+        z = np.ascontiguousarray(np.asarray(values, dtype=np.complex128))
+        assert self.L.ref_save_cdata(z.size, z.view(np.float64), fname.encode()) == 0
+
+    def parse_cdata(self, text, n):
+        out = np.zeros(2 * n)
+        self.L.ref_parse_cdata(n, text.encode(), out)
+        return out.view(np.complex128)
+
+    def random_function(self, kind, d, n, nseed, nbin, xmin, xmax, model="maximum", params=(), shape="ball",
+                        ratio=1.0):
+        data = np.zeros(nseed * nbin)
+        args = self._med(d, n, model, params, shape, ratio, 1)[:-1]
+        self.L.ref_random_function({"crsec": 0, "dos": 1}[kind], *args, nseed, nbin, xmin, xmax, data)
+        return data.reshape(nbin, nseed)
 
     def solve_aberth(self, d, n, seed, dom, z0, model="maximum", params=(), nexpsup=4, maxit=30, toler=1e-10,
                      shape="ball", ratio=1.0):

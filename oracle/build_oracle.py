@@ -19,7 +19,7 @@ REF_ROOT = "/root/reference"
 REF_SOURCES = [
     "ms_matrix_util.c", "green_bessel.c", "medium_util.c", "nru_random.c",
     "scattering_model_util.c", "real_vector_util.c", "complex_vector_util.c",
-    "common_util.c", "root_finder.c", "domain_util.c",
+    "common_util.c", "root_finder.c", "domain_util.c", "complex_data_util.c",
 ]
 
 

@@ -8,12 +8,16 @@
 #include <stdlib.h>
 #include <string.h>
 #include <complex.h>
+#include <math.h>
 #include "dcomplex_type.h"
 #include "medium_type.h"
 #include "medium_util.h"
 #include "green_bessel.h"
 #include "ms_matrix_util.h"
 #include "root_finder.h"
+#include "real_vector_util.h"
+#include "complex_data_type.h"
+#include "complex_data_util.h"
 #include "scattering_model_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
@@ -141,4 +145,48 @@ void ref_wavefunction(int d, int n, int mtype, int np, const double* p, int shap
     }
     free(r); free(a); free(ipiv);
     drop_medium(&med);
+}
+
+/* run_random_function_omp (ms_core.c:476-519) over the reference's own
+ * fill_medium, total_cross_section and dk_log_det_ms: seed g+1 for sample g,
+ * the k grid of get_arg_rfun (random_function_util.c:103), each bin sorted by
+ * sort_vector (sort_random_function, random_function_util.c:110). */
+void ref_random_function(int type, int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                         int nseed, int nbin, double xmin, double xmax, double* data) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, 1);
+    for (int g = 0; g < nseed; g++) {
+        fill_medium(&med, g + 1);
+        for (int i = 0; i < nbin; i++) {
+            double k = xmin * exp(i * log(xmax / xmin) / (nbin - 1));
+            data[g + i * nseed] = type == 0 ? total_cross_section(&med, k)
+                                            : -cimag(dk_log_det_ms(&med, k)) / (2 * k * 3.1415926535897932385);
+        }
+    }
+    for (int i = 0; i < nbin; i++) sort_vector(nseed, data + i * nseed);
+    drop_medium(&med);
+}
+
+/* save_cdata (complex_data_util.c:21-28) of n values into a new file */
+int ref_save_cdata(int n, const double* data, const char* fname) {
+    FILE* fp = fopen(fname, "w");
+    if (!fp) return -1;
+    ComplexData cd;
+    memset(&cd, 0, sizeof cd);
+    cd.ntot = n;
+    cd.data = (dcomplex*)data;
+    save_cdata(&cd, fp);
+    fclose(fp);
+    return 0;
+}
+
+/* parse_cdata (complex_data_util.c:35) of a data string back into n values */
+void ref_parse_cdata(int n, const char* text, double* data) {
+    ComplexData cd;
+    memset(&cd, 0, sizeof cd);
+    cd.ntot = n;
+    cd.data = (dcomplex*)data;
+    char* copy = strdup(text);
+    parse_cdata(&cd, copy);
+    free(copy);
 }

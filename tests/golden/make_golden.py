@@ -146,6 +146,10 @@ def reference_runs():
     # total cross section (zgesv path)
     for k in (0.5, 2.0):
         add("total_cross_section", d=3, n=120, seed=9, k=k, out=r.total_cross_section(3, 120, 9, k))
+    # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
+    for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
+        data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
+        add("random_function", type=kind, d=d, n=n, nseed=5, nbin=4, xmin=0.4, xmax=3.5, data=data.tolist())
     return runs
 
 

@@ -74,3 +74,19 @@ def test_realisation_sizes_match_reference(ref_runs):
     import msmodel_gb300 as ms
     c = [c for c in ref_runs["cases"] if c["kind"] == "realisation_sizes"][0]
     assert ms.realisation_sizes(len(c["sizes"]), seed=c["seed"]) == c["sizes"]
+
+
+def test_tuning_table_host_side():
+    """The launch-choice table is host state: set, query, save and load without a GPU."""
+    import msmodel_gb300 as ms
+    try:
+        ms.tune_set("dlogf", "mixed", 300, "fp64", 1)
+        assert ms.tune_get("dlogf", "mixed", 400) == ("fp64", 1)   # same bucket (256, 512]
+        assert ms.tune_get("dlogf", "mixed", 600) == (None, 0)     # next bucket untouched
+        with pytest.raises(ms.MsgpuError):
+            ms.tune_set("tracelog", "fp64", 64, "mixed", 0)        # FP64 requests stay FP64
+        rows = ms.tune_table()
+        assert ("dlogf", "mixed", 512, "fp64", 1) in [tuple(r) for r in rows]
+    finally:
+        ms.tune_set("dlogf", "mixed", 300, None, 0)
+    assert ms.tune_table() == []

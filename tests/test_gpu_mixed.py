@@ -108,6 +108,23 @@ def test_double_float_elements(ms, oracle):
     assert np.max(rel(dm, dwant)) < 1e-13
 
 
+def test_double_float_elements_fp32_pipe(ms, oracle):
+    """The d=3 elements entirely in double-float (r, phase and growth
+    reductions included), as the mixed engine assembles them: within
+    |k r| * 2^-46 + 1e-13 relative of the FP64 Green function (the phase
+    carries the double-float rounding of r and k r)."""
+    rng = np.random.default_rng(12)
+    ks = rng.uniform(0.05, 6.0, 800) + 1j * rng.uniform(-1.5, 0.2, 800)
+    rs = rng.uniform(0.2, 40.0, 800)
+    m = ms.eval_special(7, 3, ks, rs)
+    dm = ms.eval_special(8, 3, ks, rs)
+    want = -np.array([oracle.free_green(3, k, r) for k, r in zip(ks, rs)])
+    dwant = -np.array([oracle.dk_free_green(3, k, r) for k, r in zip(ks, rs)])
+    bound = np.abs(ks) * rs * 2.0 ** -46 + 1e-13
+    assert np.all(rel(m, want) < bound)
+    assert np.all(rel(dm, dwant) < bound)
+
+
 def test_mixed_amplitudes_refined(ms, oracle):
     """Mixed LU plus FP64 iterative refinement: the amplitudes a = M^-1 phi reach
     an FP64 residual |phi - M a| / |phi| <= 1e-12 (checked on the host with the

@@ -35,3 +35,40 @@ def test_wavefunction_d2_seed_average(ms, oracle):
         d_acc += np.abs(p) ** 2
     assert np.max(np.abs(fun - f_acc / 3)) < 1e-10 * np.max(np.abs(f_acc))
     assert np.max(np.abs(den - d_acc / 3)) < 1e-9 * np.max(d_acc)
+
+
+def test_wave_batch_equals_single_k(ms):
+    """All (medium, k) solves in one job give the per-k results bit for bit."""
+    media = [ms.Medium(3, 90, seed=s) for s in (1, 2)]
+    ks = [1.1 + 0j, 2.2 - 0.1j, 0.7 + 0j]
+    dom = [-3.0, 3.0, -2.5, 2.5]
+    fb, db, pb, ab = ms.wave_function_batch(media, ks, 9, 7, dom)
+    for i, k in enumerate(ks):
+        f, d, p, a = ms.wave_function(media, k, 9, 7, dom)
+        assert np.array_equal(f, fb[i]) and np.array_equal(d, db[i]) and np.array_equal(p, pb[i])
+        for m in range(len(media)):
+            assert np.array_equal(a[m], ab[m][i])
+
+
+def _psi_fp64(pos, amps, k, nx, ny, dom):
+    """psi = e^{ikx} + sum_i a_i G(k, r_i), G = -e^{ikr}/(4 pi r), FP64 numpy."""
+    xs = dom[0] + (dom[1] - dom[0]) / (nx - 1) * (np.arange(nx * ny) % nx)
+    ys = dom[3] - (dom[3] - dom[2]) / (ny - 1) * (np.arange(nx * ny) // nx)
+    p = pos.reshape(-1, 3)
+    r = np.sqrt((p[None, :, 0] - xs[:, None]) ** 2 + (p[None, :, 1] - ys[:, None]) ** 2 + p[None, :, 2] ** 2)
+    g = -np.exp(1j * k * r) / (4 * np.pi * r)
+    return np.exp(1j * k * xs) + g @ amps, np.abs(g) @ np.abs(amps)
+
+
+@pytest.mark.parametrize("k", [1.5 + 0j, 2.9 + 0j, 0.8 - 0.4j, 2.0 + 0.3j])
+def test_double_float_grid(ms, k):
+    """d = 3 grid in double-float arithmetic (mixed precision): psi against an
+    FP64 evaluation with the same amplitudes, within 1e-12 of sum |a_i G_i|."""
+    n = 400
+    med = ms.Medium(3, n, seed=3)
+    rad = (n / (4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
+    dom = [-1.2 * rad, 1.2 * rad, -rad, rad]
+    _, _, psi, amps = ms.wave_function(med, k, 23, 19, dom, precision="mixed")
+    want, scale = _psi_fp64(med.pos, amps[0], k, 23, 19, dom)
+    err = np.max(np.abs(psi - want) / scale)
+    assert err < 1e-12, err
