@@ -317,7 +317,9 @@ def workload_map2d(ms, torch, args):
     osub, _ = ms.tracelog_batch([med], sub, precision="mixed")
     lnd64, lndm = o64 * 2048, osub * 2048
     err = np.abs(lndm.real - lnd64.real) / np.abs(lnd64.real)
-    return {"workload": f"kplane d=2 N=2048 256x256 Re[0.5,4] Im[-0.3,0] (mixed on {len(kmix)} points)",
+    stats = ms.engine_stats() if os.environ.get("MSGPU_STATS") else None
+    return {**({"phase_cycles_last_mixed_job": stats} if stats else {}),
+            "workload": f"kplane d=2 N=2048 256x256 Re[0.5,4] Im[-0.3,0] (mixed on {len(kmix)} points)",
             "unit": "evals/s", "mixed": vmx, "fp64": v64, "ratio": vmx / v64,
             "mixed_lndet_rel_err_subgrid": {"max": float(err.max()), "median": float(np.median(err)),
                                             "points": int(err.size)},
@@ -372,17 +374,23 @@ def workload_wave(ms, torch, args):
     dom = [-rad, rad, -rad, rad]
     ks = 0.5 + 2.5 * np.arange(nk) / max(nk - 1, 1) + 0j
     res = {}
-    for prec in ("mixed", "fp64"):
+    for prec in args.legs.split(","):
         (f, d, _, a), el = _wall(torch, lambda: ms.wave_function_batch([med], ks, npx, npx, dom, prec,
                                                                        want_psi=False))
         res[prec] = (f, a[0], el)
+    line = {"workload": f"wavefunction d=3 N=4096 {nk} real k in [0.5,3], {npx}x{npx} grid z=0", "unit": "k/s"}
+    for prec, (_, _, el) in res.items():
+        line[prec] = nk / el
+        line[prec + "_seconds"] = el
+    if "mixed" in res:
+        line["pair_evals_per_s_mixed"] = nk * npx * npx * n / res["mixed"][2]
+    if len(res) < 2:
+        return line
     f_m, a_m, el_m = res["mixed"]
     f_d, a_d, el_d = res["fp64"]
-    line = {"workload": f"wavefunction d=3 N=4096 {nk} real k in [0.5,3], {npx}x{npx} grid z=0",
-            "unit": "k/s", "mixed": nk / el_m, "fp64": nk / el_d, "mixed_seconds": el_m, "fp64_seconds": el_d,
-            "pair_evals_per_s_mixed": nk * npx * npx * n / el_m,
-            "fun_max_abs_diff_vs_fp64": float(np.max(np.abs(f_m - f_d))),
-            "amp_max_rel_diff_vs_fp64": float(np.max(np.abs(a_m - a_d)) / np.max(np.abs(a_d)))}
+    line["fun_max_abs_diff_vs_fp64"] = float(np.max(np.abs(f_m - f_d)))
+    line["fun_max_abs"] = float(np.max(np.abs(f_d)))
+    line["amp_max_rel_diff_vs_fp64"] = float(np.max(np.abs(a_m - a_d)) / np.max(np.abs(a_d)))
     if not args.no_cpu:
         from oracle import Oracle
         o = Oracle()
@@ -391,19 +399,23 @@ def workload_wave(ms, torch, args):
             m = o.ms_matrix(3, n, med.pos, ks[j])
             phi = np.exp(1j * ks[j] * med.pos[0::3])
             for prec, a in (("mixed", a_m), ("fp64", a_d)):
-                worst[prec] = max(worst[prec], float(np.max(np.abs(phi - m @ a[j])) / np.max(np.abs(phi))))
+                r = np.max(np.abs(phi - m @ a[j]))
+                worst[prec] = max(worst[prec], float(r / np.max(np.abs(phi))))
+                # normwise backward error |phi - M a| / (|M| |a| + |phi|), infinity norms
+                bw = r / (np.max(np.sum(np.abs(m), axis=1)) * np.max(np.abs(a[j])) + np.max(np.abs(phi)))
+                worst[prec + "_backward"] = max(worst.get(prec + "_backward", 0.0), float(bw))
         line["residual_max"] = worst
-        # the reference's per-k cost: the N=4096 solve (2x2 grid) plus the grid (32x32 minus 2x2, per pixel)
+        # the reference's per-k cost: the N=4096 solve (2x2 grid) plus the grid (192x192 minus 2x2, per pixel)
         t0 = time.perf_counter()
         o.wavefunction(3, n, med.pos, ks[nk // 2], 2, 2, dom, nthreads=os.cpu_count())
         t_solve = time.perf_counter() - t0
         t0 = time.perf_counter()
-        o.wavefunction(3, n, med.pos, ks[nk // 2], 32, 32, dom, nthreads=os.cpu_count())
-        t_px = max(time.perf_counter() - t0 - t_solve, 0.0) / (32 * 32 - 4)
+        o.wavefunction(3, n, med.pos, ks[nk // 2], 192, 192, dom, nthreads=os.cpu_count())
+        t_px = max(time.perf_counter() - t0 - t_solve, 0.0) / (192 * 192 - 4)
         per_k = t_solve + t_px * npx * npx
         line["cpu_baseline"] = {"value": 1.0 / per_k, "unit": "k/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"one k: N=4096 zgesv {t_solve:.2f} s + {t_px * 1e6:.1f} us per pixel "
-                                          f"(32x32 grid), scaled to {npx}x{npx} pixels"}
+                                "sample": f"one k: N=4096 zgesv {t_solve:.2f} s + {t_px * 1e6:.2f} us per pixel "
+                                          f"(192x192 grid), scaled to {npx}x{npx} pixels"}
     return line
 
 
@@ -478,6 +490,7 @@ def main():
     ap.add_argument("--count", type=int, default=0, help="aberth workload: realisations (default 4096)")
     ap.add_argument("--fp64-count", type=int, default=64, help="aberth workload: realisations searched in FP64")
     ap.add_argument("--nk-wave", type=int, default=256, help="wave workload: wave numbers")
+    ap.add_argument("--legs", default="mixed,fp64", help="wave workload: precisions to run")
     ap.add_argument("--sample", type=float, default=0.0, help="map2d workload: fraction of the map (default all)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -45,6 +45,15 @@ MSG_HD zc operator/(zc a, zc b) {
     }
 }
 MSG_HD zc operator/(double s, zc b) { return zc{s, 0.0} / b; }
+// 1 / b with Smith's scaling in two real divisions (the quotient above takes three)
+MSG_HD zc zrecip(zc b) {
+    if (fabs(b.re) >= fabs(b.im)) {
+        const double r = b.im / b.re, d = 1.0 / (b.re + b.im * r);
+        return zc{d, -r * d};
+    }
+    const double r = b.re / b.im, d = 1.0 / (b.re * r + b.im);
+    return zc{r * d, -d};
+}
 MSG_HD zc& operator/=(zc& a, zc b) { a = a / b; return a; }
 
 MSG_HD zc zexp(zc z) {

@@ -35,6 +35,31 @@ MSG_HD double uball_surface(int d) {
     return s;
 }
 
+// Scalar coefficients of the K_nu loops for nu = 0, 1 (the orders the
+// Foldy-Lax matrix and its k-derivative need), computed at compile time by the
+// same double operations the loops would do; the FP64 pipe (1/64 of the FP32
+// rate on GB300) then spends no division per iteration on them.
+constexpr int BK_TAB = 128;
+struct BkTables {
+    double asym[2][BK_TAB];    // (4 nu^2 - (2k-1)^2) / k
+    double ser_t[2][BK_TAB];   // 1 / (k (nu + k))
+    double ser_c[2][BK_TAB];   // (1/k + 1/(nu + k)) / 2
+    double miller[2][BK_TAB];  // j / ((j - nu - 1/2)(j + nu - 1/2))
+};
+constexpr BkTables make_bk_tables() {
+    BkTables t{};
+    for (int nu = 0; nu < 2; ++nu)
+        for (int k = 1; k < BK_TAB; ++k) {
+            const double o = 2.0 * k - 1.0, fn = 4.0 * nu * nu;
+            t.asym[nu][k] = (fn - o * o) / k;
+            t.ser_t[nu][k] = 1.0 / ((double)k * (nu + k));
+            t.ser_c[nu][k] = 0.5 * (1.0 / k + 1.0 / (nu + k));
+            t.miller[nu][k] = (double)k / ((k - nu - 0.5) * (k + nu - 0.5));
+        }
+    return t;
+}
+__constant__ BkTables c_bk = make_bk_tables();
+
 // B_nu(z) = K_nu(z) / (sqrt(pi/2z) e^-z), asymptotic series (DLMF 10.40.2)
 // truncated at the smallest term (index |2z|) or once |term| < 1e-16.
 MSG_D zc bk_asym(int nu, zc z) {
@@ -44,7 +69,7 @@ MSG_D zc bk_asym(int nu, zc z) {
     zc iz8 = 1.0 / (8.0 * z);
     for (int k = 1; k < kmax; k++) {
         double o = 2.0 * k - 1.0;
-        term = term * iz8 * ((fn - o * o) / k);
+        term = term * iz8 * ((nu < 2 && k < BK_TAB) ? c_bk.asym[nu][k] : (fn - o * o) / k);
         sum += term;
         if (zabs2(term) < 1e-32) break;
     }
@@ -78,9 +103,10 @@ MSG_D zc bk_series(int n, zc z) {
     zc t = mk(1.0 / nfact);
     for (int j = 0; j < n; j++) t = t * h;
     zc sum = c * t;
+    const bool tab = n < 2;
     for (int k = 1; k < 50; k++) {
-        t = t * q * (1.0 / ((double)k * (n + k)));
-        c = c - 0.5 * (1.0 / k + 1.0 / (n + k));
+        t = t * q * (tab ? c_bk.ser_t[n][k] : 1.0 / ((double)k * (n + k)));
+        c = c - (tab ? c_bk.ser_c[n][k] : 0.5 * (1.0 / k + 1.0 / (n + k)));
         zc add = c * t;
         sum += add;
         if (zabs2(add) < 1e-32 * zabs2(sum)) break;
@@ -96,10 +122,12 @@ MSG_D zc bk_miller(int nu, zc z) {
     double x = z.re + (-LN_EPS);
     int jmax = (int)floor(x * x / (4.0 * (z.re + zabs(z))));
     zc ratio = mk(1.0), s = mk(0.0);
+    zc inv = mk(1.0);  // 1 / ratio: one complex reciprocal per step serves both quotients
     for (int j = jmax; j > 0; j--) {
-        double c = (double)j / ((j - nu - 0.5) * (j + nu - 0.5));
-        ratio = c * (2.0 * (z + (double)j) - (double)(j + 1) / ratio);
-        s = 1.0 + s / ratio;
+        const double c = (nu < 2 && j < BK_TAB) ? c_bk.miller[nu][j] : (double)j / ((j - nu - 0.5) * (j + nu - 0.5));
+        ratio = c * (2.0 * (z + (double)j) - (double)(j + 1) * inv);
+        inv = zrecip(ratio);
+        s = 1.0 + s * inv;
     }
     return 1.0 / s;
 }

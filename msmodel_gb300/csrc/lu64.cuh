@@ -422,6 +422,48 @@ __device__ __forceinline__ void pair_elements(int d, zc k, double r, bool want_d
     if (want_deriv) dm = -dk_free_green(d, k, r);
 }
 
+// K_nu regime of the pair's argument z = -i k r (the reference's switch,
+// green_bessel.c:208-218): 0 asymptotic, 1 ascending series, 2 Miller.
+__device__ __forceinline__ int k_regime(zc k, double r) {
+    const double x = k.im * r, y = -k.re * r;
+    if (x * x + y * y > 256.0) return 0;
+    if (x < 3.0 - y * y / 12.0) return 1;
+    return 2;
+}
+
+// Pairs i < j of the 32 x 32 tile (I, J) for d != 3, evaluated grouped by K_nu
+// regime: the three loops differ several-fold in length, and a warp that
+// mixes them runs all of them.  Every pair goes to one of three lists in
+// shared memory (list: 3 x 1024 entries, cnt: 3 counters, both zero on entry
+// and on return), then consecutive threads take consecutive list entries;
+// put(ii, jj, m, dm) receives each element.  Entries of a list are in no
+// fixed order, but every element is a function of (k, r) alone.
+template <class Put>
+__device__ __forceinline__ void tile_pairs_grouped(int I, int J, int n, int d, const double* __restrict__ pos, zc k,
+                                                   bool want_deriv, unsigned short* list, int* cnt, Put put) {
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int p = tid + NT * q, ii = p & 31, jj = p >> 5;
+        const int i = I * 32 + ii, j = J * 32 + jj;
+        if (i < n && j < n && i < j) {
+            const int reg = k_regime(k, atom_distance(d, pos, i, j));
+            list[reg * 1024 + atomicAdd(&cnt[reg], 1)] = (unsigned short)p;
+        }
+    }
+    __syncthreads();
+    const int c0 = cnt[0], c1 = cnt[1], tot = c0 + c1 + cnt[2];
+    for (int w = tid; w < tot; w += NT) {
+        const int p = w < c0 ? list[w] : (w < c0 + c1 ? list[1024 + w - c0] : list[2048 + w - c0 - c1]);
+        const int ii = p & 31, jj = p >> 5;
+        zc m, dm = mk(0.0);
+        pair_elements(d, k, atom_distance(d, pos, I * 32 + ii, J * 32 + jj), want_deriv, m, dm);
+        put(ii, jj, m, dm);
+    }
+    __syncthreads();
+    if (tid < 3) cnt[tid] = 0;
+}
+
 // Assemble M(k) into A and, if B != nullptr, dM/dk into B (ld n, column-major).
 // Tiles of 32 x 32 pairs above the diagonal are evaluated once and written to
 // both triangles, the mirrored tile through shared memory to keep stores coalesced.
@@ -435,9 +477,30 @@ static __device__ void assemble(zc* __restrict__ A, zc* __restrict__ B, int n, i
     __syncthreads();
     const zc dg0 = s.diag[0], dg1 = s.diag[1];
     zc (*T2)[NB + 1] = reinterpret_cast<zc(*)[NB + 1]>(&s.As[0][0]);
+    // d != 3: pair lists of the regime grouping in the (idle) U12 tile buffer
+    unsigned short* list = reinterpret_cast<unsigned short*>(&s.Bs[0][0]);
+    int* cnt = reinterpret_cast<int*>(list + 3 * 1024);
+    const bool grouped = d != 3 && d != 1;
+    if (grouped && tid < 3) cnt[tid] = 0;
+    __syncthreads();
     const int nt = (n + 31) / 32;
     for (int J = 0; J < nt; ++J) {
         for (int I = 0; I <= J; ++I) {
+            if (grouped) {
+                tile_pairs_grouped(I, J, n, d, pos, k, B != nullptr, list, cnt, [&](int ii, int jj, zc m, zc dm) {
+                    s.T[jj][ii] = m;
+                    if (B) T2[jj][ii] = dm;
+                });
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+                    const int i = I * 32 + ii, j = J * 32 + jj;
+                    if (i < n && j < n && i <= j) {
+                        A[i + (size_t)j * n] = i < j ? s.T[jj][ii] : dg0;
+                        if (B) B[i + (size_t)j * n] = i < j ? T2[jj][ii] : dg1;
+                    }
+                }
+            } else {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
@@ -457,6 +520,7 @@ static __device__ void assemble(zc* __restrict__ A, zc* __restrict__ B, int n, i
                         T2[jj][ii] = dm;
                     }
                 }
+            }
             }
             __syncthreads();
 #pragma unroll

@@ -54,6 +54,9 @@ struct MixPanel {
     Df3Tables tab;
     float4 ci[NB], cj[NB];  // x.h x.l y.h y.l
     float2 ciz[NB], cjz[NB];
+    // assembly of d != 3: pair lists of the K_nu regime grouping
+    unsigned short list[3 * 1024];
+    int cnt[4];
 };
 struct MixGemm {
     uint8_t A[A_BAND];
@@ -286,6 +289,8 @@ __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __
     const int q = warp & 3, hcol = warp >> 2;  // TMEM lane quadrant, column half of this warp
     const int rloc = 32 * q + lane;
     while (bi < nbi) {
+        int nbi2 = bi, nbj2 = bj;
+        next_tile(nbi2, nbj2);
         // this thread's row and 16 columns of C, and their exponents, fetched before
         // the MMAs complete so the memory latency hides behind the tensor core
         const int row = bi * MT_M + rloc;
@@ -312,8 +317,6 @@ __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __
         const bool mw = mbar_wait(&s.bar_mma, ph.mma);
         ph.mma ^= 1;
         if (!mw && lane == 0) s.err = 1;
-        int nbi2 = bi, nbj2 = bj;
-        next_tile(nbi2, nbj2);
         if (tid == 0 && nbi2 < nbi) {  // operands of the next tile: smem is free once the MMAs completed
             if (nbi2 != bi) {
                 mbar_arrive_expect_tx(&s.bar_a, A_BAND);
@@ -677,10 +680,10 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
     const bool d3 = d == 3;
     const df kr = df_from_double(k.re), ki = df_from_double(k.im);
     const bool grow = k.im != 0.0;
-    if (d3) {
-        df3_tables_init(s.u.p.tab);
-        __syncthreads();
-    }
+    const bool grouped = d != 3 && d != 1;
+    if (d3) df3_tables_init(s.u.p.tab);
+    if (grouped && tid < 3) s.u.p.cnt[tid] = 0;
+    __syncthreads();
     float mx = 0.0f;
     auto cvt = [](zc v) {
         df a = df_from_double(v.re), b = df_from_double(v.im);
@@ -709,6 +712,38 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                 }
                 __syncthreads();
             }
+            if (grouped) {
+                tile_pairs_grouped(I, J, n, d, pos, k, B != nullptr, s.u.p.list, s.u.p.cnt,
+                                   [&](int ii, int jj, zc m, zc dm) {
+                                       const float4 fm = cvt(m);
+                                       mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                                       s.u.p.T[jj][ii] = fm;
+                                       if (B) {
+                                           const float4 fd = cvt(dm);
+                                           mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                                           s.u.p.T2[jj][ii] = fd;
+                                       }
+                                   });
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+                    const int i = I * 32 + ii, j = J * 32 + jj;
+                    if (i < n && j < n && i <= j) {
+                        float4 fm = s.u.p.T[jj][ii], fd = make_float4(0, 0, 0, 0);
+                        if (B) fd = s.u.p.T2[jj][ii];
+                        if (i == j) {
+                            fm = cvt(dg0);
+                            mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                            if (B) {
+                                fd = cvt(dg1);
+                                mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                            }
+                        }
+                        A[i + (size_t)j * n] = fm;
+                        if (B) B[i + (size_t)j * n] = fd;
+                    }
+                }
+            } else {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
@@ -747,6 +782,7 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                         s.u.p.T2[jj][ii] = fd;
                     }
                 }
+            }
             }
             __syncthreads();
 #pragma unroll
@@ -857,10 +893,26 @@ __device__ void df_solve_vec(const float4* __restrict__ A, float4* __restrict__ 
 }
 
 // a = M^-1 phi by the mixed LU plus iterative refinement: r = phi - M a with
-// the double-float copy of M, a += (LU)^-1 r in FP64, until |r|/|phi| <= 1e-13
-// (max norms) or 6 corrections.  Returns sigma = -Im(conj(phi).a)/k (the
-// optical theorem of total_cross_section, ms_matrix_util.c:361).
-__device__ zc refine_solve(const float4* __restrict__ LU, const float4* __restrict__ M, const zc* __restrict__ phi,
+// M in FP64 for the refinement residual: every element evaluated as the FP64
+// engine does (each pair on its own, so the writes stay coalesced)
+__device__ void assemble_fp64_copy(zc* __restrict__ M, const MedDev& md, zc k, MixSmem& s) {
+    const int n = md.n;
+    const zc dg = s.diag[0];
+    for (size_t e = threadIdx.x; e < (size_t)n * n; e += NT) {
+        const int i = (int)(e % n), j = (int)(e / n);
+        zc m = dg, dm;
+        if (i != j) pair_elements(md.d, k, atom_distance(md.d, md.pos, min(i, j), max(i, j)), false, m, dm);
+        M[e] = m;
+    }
+    __syncthreads();
+}
+
+// a = M^-1 phi from the mixed LU with iterative refinement: r = phi - M a in
+// FP64 against the FP64 copy of M, a += (LU)^-1 r (correction in double-float,
+// a kept in FP64), until |r| <= 1e-14 |phi| (max norms), the residual stops
+// halving, or 8 corrections.  Returns sigma = -Im(conj(phi).a)/k (the optical
+// theorem of total_cross_section, ms_matrix_util.c:361).
+__device__ zc refine_solve(const float4* __restrict__ LU, const zc* __restrict__ M, const zc* __restrict__ phi,
                            zc* __restrict__ x, float4* __restrict__ r, float4* __restrict__ t, const MedDev& md,
                            zc k, const int* __restrict__ ipiv, MixSmem& s) {
     const int n = md.n, tid = threadIdx.x;
@@ -882,21 +934,25 @@ __device__ zc refine_solve(const float4* __restrict__ LU, const float4* __restri
     block_argmax(pmax, tid, s, dummy);
     pmax = block_max_value(s);
     __syncthreads();
-    for (int it = 0; it < 6; ++it) {
-        // r = phi - M x, rows over threads (coalesced columns of M); x as double-floats in t
-        for (int i = tid; i < n; i += NT) t[i] = to4(x[i]);
-        __syncthreads();
+    double prev = INFINITY;
+    for (int it = 0; it < 8; ++it) {
+        // r = phi - M x in FP64, rows over threads (coalesced columns of M)
         double rmax = 0.0;
         for (int i = tid; i < n; i += NT) {
-            dfc acc = dfc{df_from_double(phi[i].re), df_from_double(phi[i].im)};
-            for (int j = 0; j < n; ++j) acc = dfc_fms(acc, dfc_load(M + i + (size_t)j * n), dfc_load(t + j));
-            dfc_store(r + i, acc);
-            rmax = fmax(rmax, fabs(df_to_double(acc.re)) + fabs(df_to_double(acc.im)));
+            zc acc = phi[i];
+            for (int j = 0; j < n; ++j) {
+                const zc mv = M[i + (size_t)j * n], xv = x[j];
+                acc.re = fma(-mv.re, xv.re, fma(mv.im, xv.im, acc.re));
+                acc.im = fma(-mv.re, xv.im, fma(-mv.im, xv.re, acc.im));
+            }
+            r[i] = to4(acc);
+            rmax = fmax(rmax, fabs(acc.re) + fabs(acc.im));
         }
         block_argmax(rmax, tid, s, dummy);
         rmax = block_max_value(s);
         __syncthreads();
-        if (!(rmax > 1e-13 * pmax)) break;
+        if (!(rmax > 1e-14 * pmax) || !(rmax < 0.5 * prev)) break;
+        prev = rmax;
         df_solve_vec(LU, r, n, ipiv, s);
         for (int i = tid; i < n; i += NT) {
             const dfc v = dfc_load(r + i);
@@ -941,7 +997,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
     float4* A = reinterpret_cast<float4*>(P.ws) + (size_t)blockIdx.x * slot_all;
     float4* B = (P.kind == 1) ? A + P.slot : nullptr;
     // kind 2: copy of M, right-hand side phi, solution, residual, correction
-    float4* Mc = A + P.slot;
+    zc* Mc = reinterpret_cast<zc*>(A + P.slot);  // kind 2: M in FP64 for the refinement
     zc* vphi = reinterpret_cast<zc*>(A + 2 * P.slot);
     zc* vx = vphi + vec;
     float4* vr = reinterpret_cast<float4*>(vx + vec);
@@ -975,7 +1031,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         } else {
             if (P.kind == 2) {
                 // keep M for the residual; incident plane wave along +x (incident_wave_util.c:76)
-                for (size_t e = tid; e < (size_t)md.n * md.n; e += NT) Mc[e] = A[e];
+                assemble_fp64_copy(Mc, md, k, s);
                 for (int i = tid; i < md.n; i += NT) vphi[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
                 __syncthreads();
             }
