@@ -318,7 +318,18 @@ def workload_map2d(ms, torch, args):
     lnd64, lndm = o64 * 2048, osub * 2048
     err = np.abs(lndm.real - lnd64.real) / np.abs(lnd64.real)
     stats = ms.engine_stats() if os.environ.get("MSGPU_STATS") else None
-    return {**({"phase_cycles_last_mixed_job": stats} if stats else {}),
+    cpu = None
+    if not args.no_cpu:
+        from oracle import Oracle
+        o = Oracle()
+        th = os.cpu_count() or 1
+        sample = sub[:2 * th]
+        t0 = time.perf_counter()
+        o.tracelog_batch(2, 2048, med.pos, sample, nthreads=th)
+        el = time.perf_counter() - t0
+        cpu = {"value": len(sample) / el, "unit": "evals/s", "cores": th, "kind": "port",
+               "sample": f"{len(sample)} points of the 16x16 subgrid, {th} OpenMP threads x 1 OpenBLAS thread"}
+    return {**({"phase_cycles_last_mixed_job": stats} if stats else {}), **({"cpu_baseline": cpu} if cpu else {}),
             "workload": f"kplane d=2 N=2048 256x256 Re[0.5,4] Im[-0.3,0] (mixed on {len(kmix)} points)",
             "unit": "evals/s", "mixed": vmx, "fp64": v64, "ratio": vmx / v64,
             "mixed_lndet_rel_err_subgrid": {"max": float(err.max()), "median": float(np.median(err)),

@@ -297,6 +297,7 @@ struct msgpu_job {
     double flops = 0.0;
     int grid = 0;
     std::vector<int> med_n;  // n of every medium (host copy)
+    bool d3only = true;      // every medium has d = 3
     MedDev* d_media = nullptr;
     double* d_pos = nullptr;
     double* d_ks = nullptr;
@@ -501,6 +502,7 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
         }
         J->nmax = std::max(J->nmax, m.n);
         J->med_n[i] = m.n;
+        if (m.d != 3) J->d3only = false;
         npos += (size_t)m.n * m.d;
     }
     auto fail = [&](const char* what) -> msgpu_job* {
@@ -591,7 +593,7 @@ static int launch_locked(msgpu_job* J, void* ws, cudaStream_t st) {
     P.amps = J->d_amps;
     P.amp_off = J->d_amp_off;
     if (J->precision == MSGPU_MIXED) {
-        int e = mixed_run(P, J->grid, J->nmax, st);
+        int e = mixed_run(P, J->grid, J->nmax, J->d3only, st);
         if (e) return set_err(e, "mixed engine launch failed");
         return 0;
     }

@@ -37,7 +37,8 @@ void count_launches(int n);
 
 // Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
 // negative MSGPU_E* code on error.
-int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st);
+// d3only: every medium of the job has d = 3 (selects the d = 3 kernel instantiation).
+int mixed_run(const EngineParams& P, int grid, int nmax, bool d3only, cudaStream_t st);
 // Allocates the mixed engine's scratch for `grid` CTAs and matrices up to nmax
 // (mixed_run does so itself; called before a stream capture, which must not allocate).
 int mixed_prepare(int grid, int nmax);

@@ -668,6 +668,50 @@ __device__ bool trace_solve_mixed(const float4* __restrict__ A, float4* __restri
 }
 
 // assembly in FP64, stored double-float; returns the largest |entry| seen
+// One 32 x 32 tile of a d != 3 matrix (K_nu elements, FP64, grouped by regime)
+// stored as double-floats: the direct triangle here, the mirror by the caller.
+// Not inlined, so that d = 3 matrices keep the kernel's registers for themselves.
+__device__ __noinline__ float assemble_tile_grouped(float4* __restrict__ A, float4* __restrict__ B, int n, int d,
+                                                   const double* __restrict__ pos, zc k, int I, int J, zc dg0,
+                                                   zc dg1, MixSmem& s, float mx) {
+    const int tid = threadIdx.x;
+    auto cvt = [](zc v) {
+        df a = df_from_double(v.re), b = df_from_double(v.im);
+        return make_float4(a.h, a.l, b.h, b.l);
+    };
+    tile_pairs_grouped(I, J, n, d, pos, k, B != nullptr, s.u.p.list, s.u.p.cnt, [&](int ii, int jj, zc m, zc dm) {
+        const float4 fm = cvt(m);
+        mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+        s.u.p.T[jj][ii] = fm;
+        if (B) {
+            const float4 fd = cvt(dm);
+            mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+            s.u.p.T2[jj][ii] = fd;
+        }
+    });
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+        const int i = I * 32 + ii, j = J * 32 + jj;
+        if (i < n && j < n && i <= j) {
+            float4 fm = s.u.p.T[jj][ii], fd = make_float4(0, 0, 0, 0);
+            if (B) fd = s.u.p.T2[jj][ii];
+            if (i == j) {
+                fm = cvt(dg0);
+                mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                if (B) {
+                    fd = cvt(dg1);
+                    mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                }
+            }
+            A[i + (size_t)j * n] = fm;
+            if (B) B[i + (size_t)j * n] = fd;
+        }
+    }
+    return mx;
+}
+
+template <bool D3ONLY>
 __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int n, int d,
                              const double* __restrict__ pos, const msgpu_model& mdl, zc k, MixSmem& s) {
     const int tid = threadIdx.x;
@@ -677,10 +721,10 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
     }
     __syncthreads();
     const zc dg0 = s.diag[0], dg1 = s.diag[1];
-    const bool d3 = d == 3;
+    const bool d3 = D3ONLY || d == 3;
     const df kr = df_from_double(k.re), ki = df_from_double(k.im);
     const bool grow = k.im != 0.0;
-    const bool grouped = d != 3 && d != 1;
+    const bool grouped = !D3ONLY && d != 3 && d != 1;
     if (d3) df3_tables_init(s.u.p.tab);
     if (grouped && tid < 3) s.u.p.cnt[tid] = 0;
     __syncthreads();
@@ -713,36 +757,7 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                 __syncthreads();
             }
             if (grouped) {
-                tile_pairs_grouped(I, J, n, d, pos, k, B != nullptr, s.u.p.list, s.u.p.cnt,
-                                   [&](int ii, int jj, zc m, zc dm) {
-                                       const float4 fm = cvt(m);
-                                       mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
-                                       s.u.p.T[jj][ii] = fm;
-                                       if (B) {
-                                           const float4 fd = cvt(dm);
-                                           mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
-                                           s.u.p.T2[jj][ii] = fd;
-                                       }
-                                   });
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
-                    const int i = I * 32 + ii, j = J * 32 + jj;
-                    if (i < n && j < n && i <= j) {
-                        float4 fm = s.u.p.T[jj][ii], fd = make_float4(0, 0, 0, 0);
-                        if (B) fd = s.u.p.T2[jj][ii];
-                        if (i == j) {
-                            fm = cvt(dg0);
-                            mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
-                            if (B) {
-                                fd = cvt(dg1);
-                                mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
-                            }
-                        }
-                        A[i + (size_t)j * n] = fm;
-                        if (B) B[i + (size_t)j * n] = fd;
-                    }
-                }
+                mx = assemble_tile_grouped(A, B, n, d, pos, k, I, J, dg0, dg1, s, mx);
             } else {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -970,6 +985,12 @@ __device__ zc refine_solve(const float4* __restrict__ LU, const zc* __restrict__
     return mk(-di, 0.0) / k;
 }
 
+// One instantiation per job kind (0 ln det, 1 dlogf, 2 amplitudes) and per
+// dimension class (D3ONLY: every medium of the job has d = 3): each carries
+// only its own reduction, solve and Green function, so a kernel's registers
+// are not shaped by code it never runs (a never-taken call to the d != 3 tile
+// cost the d = 3 ln det kernel 5 %).
+template <int KIND, bool D3ONLY>
 __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScratch X) {
     extern __shared__ uint8_t smem_raw[];
     MixSmem& s = *reinterpret_cast<MixSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -993,9 +1014,9 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
     const uint32_t tmem = s.tmem;
     Phases ph{0, 0, 0};
     const size_t vec = (((size_t)P.piv_stride + 15) / 16) * 16;
-    const size_t slot_all = P.kind == 0 ? P.slot : (P.kind == 1 ? 2 * P.slot : 2 * P.slot + 4 * vec);
+    const size_t slot_all = KIND == 0 ? P.slot : (KIND == 1 ? 2 * P.slot : 2 * P.slot + 4 * vec);
     float4* A = reinterpret_cast<float4*>(P.ws) + (size_t)blockIdx.x * slot_all;
-    float4* B = (P.kind == 1) ? A + P.slot : nullptr;
+    float4* B = (KIND == 1) ? A + P.slot : nullptr;
     // kind 2: copy of M, right-hand side phi, solution, residual, correction
     zc* Mc = reinterpret_cast<zc*>(A + P.slot);  // kind 2: M in FP64 for the refinement
     zc* vphi = reinterpret_cast<zc*>(A + 2 * P.slot);
@@ -1017,7 +1038,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         const MedDev md = P.media[P.item_med[it]];
         const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
         stat_start(s);
-        const float mx = assemble_df(A, B, md.n, md.d, md.pos, md.model, k, s);
+        const float mx = assemble_df<D3ONLY>(A, B, md.n, md.d, md.pos, md.model, k, s);
         stat_add(s, PH_ASSEMBLE);
         int dummy;
         block_argmax((double)mx, tid, s, dummy);
@@ -1029,7 +1050,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
             st |= MSGPU_S_RANGE;
             res = mk(nan(""), nan(""));
         } else {
-            if (P.kind == 2) {
+            if (KIND == 2) {
                 // keep M for the residual; incident plane wave along +x (incident_wave_util.c:76)
                 assemble_fp64_copy(Mc, md, k, s);
                 for (int i = tid; i < md.n; i += NT) vphi[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
@@ -1037,9 +1058,9 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
             }
             if (!lu_mixed(A, md.n, ipiv, s, X, tmem, ph)) {
                 alive = false;
-            } else if (P.kind == 0) {
+            } else if (KIND == 0) {
                 res = tracelog_df(A, md.n, ipiv, s);
-            } else if (P.kind == 1) {
+            } else if (KIND == 1) {
                 if (!trace_solve_mixed(A, B, md.n, ipiv, s, X, tmem, ph, res)) alive = false;
             } else {
                 res = refine_solve(A, Mc, vphi, vx, vr, vt, md, k, ipiv, s);
@@ -1092,9 +1113,13 @@ unsigned long long g_mix_gen = 1;
 static int prepare_locked(int grid, int nmax, MixScratch& X) {
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(k_engine_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mixed_smem()) !=
-            cudaSuccess)
-            return MSGPU_E_CUDA;
+        const int sm = (int)mixed_smem();
+        const void* ks[6] = {(const void*)k_engine_mixed<0, false>, (const void*)k_engine_mixed<1, false>,
+                             (const void*)k_engine_mixed<2, false>, (const void*)k_engine_mixed<0, true>,
+                             (const void*)k_engine_mixed<1, true>,  (const void*)k_engine_mixed<2, true>};
+        for (const void* f : ks)
+            if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sm) != cudaSuccess)
+                return MSGPU_E_CUDA;
         attr = true;
     }
     const int nbA = (nmax + MT_M - 1) / MT_M, nbB = (nmax + MT_N - 1) / MT_N;
@@ -1138,13 +1163,22 @@ unsigned long long mixed_generation() {
     return g_mix_gen;
 }
 
-int mixed_run(const EngineParams& P, int grid, int nmax, cudaStream_t st) {
+int mixed_run(const EngineParams& P, int grid, int nmax, bool d3only, cudaStream_t st) {
     std::lock_guard<std::mutex> lk(g_mx);
     MixScratch X;
     if (int e = prepare_locked(grid, nmax, X)) return e;
     if (X.stats) cudaMemsetAsync(X.stats, 0, sizeof(unsigned long long) * PH_N, st);
     if (cudaMemsetAsync(P.counter, 0, sizeof(unsigned), st) != cudaSuccess) return MSGPU_E_CUDA;
-    k_engine_mixed<<<grid, NT, mixed_smem(), st>>>(P, X);
+    const size_t sm = mixed_smem();
+    if (d3only) {
+        if (P.kind == 0) k_engine_mixed<0, true><<<grid, NT, sm, st>>>(P, X);
+        else if (P.kind == 1) k_engine_mixed<1, true><<<grid, NT, sm, st>>>(P, X);
+        else k_engine_mixed<2, true><<<grid, NT, sm, st>>>(P, X);
+    } else {
+        if (P.kind == 0) k_engine_mixed<0, false><<<grid, NT, sm, st>>>(P, X);
+        else if (P.kind == 1) k_engine_mixed<1, false><<<grid, NT, sm, st>>>(P, X);
+        else k_engine_mixed<2, false><<<grid, NT, sm, st>>>(P, X);
+    }
     g_launches_last = 1;
     return cudaGetLastError() == cudaSuccess ? 0 : MSGPU_E_CUDA;
 }

@@ -47,6 +47,17 @@ int main(int argc, char** argv) {
     cd.get_arg = arg_cut;
     run_tracelog_omp(&med, &cd, 4);
     for (int l = 0; l < cd.ntot; l++) printf("cut %d %.17g %.17g\n", l, creal(cd.data[l]), cimag(cd.data[l]));
-    free(a); free(med.pos); free(cd.data);
+    /* total cross section, seeds 1..3, 4 log-spaced bins on [0.5, 2.5] */
+    msgpu_ref_rfun rf = {0};
+    rf.type = 0;
+    rf.nseed = 3;
+    rf.nbin = 4;
+    rf.ntot = rf.nseed * rf.nbin;
+    rf.xmin = 0.5;
+    rf.xmax = 2.5;
+    rf.data = (double*)calloc(rf.ntot, sizeof(double));
+    run_random_function_omp(&med, &rf, 4);
+    for (int l = 0; l < rf.ntot; l++) printf("rfun %d %.17g\n", l, rf.data[l]);
+    free(a); free(med.pos); free(cd.data); free(rf.data);
     return 0;
 }

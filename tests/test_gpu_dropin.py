@@ -25,10 +25,13 @@ def test_dropin_program(ms, oracle, tmp_path):
     assert out.returncode == 0, out.stderr
     vals = {}
     cut = {}
+    rfun = {}
     for line in out.stdout.splitlines():
         f = line.split()
         if f[0] == "cut":
             cut[int(f[1])] = complex(float(f[2]), float(f[3]))
+        elif f[0] == "rfun":
+            rfun[int(f[1])] = float(f[2])
         elif f[0] == "sigma":
             vals["sigma"] = float(f[1])
         else:
@@ -49,3 +52,10 @@ def test_dropin_program(ms, oracle, tmp_path):
         acc = ((s - 1) * acc + v) / s
     got = np.array([cut[l] for l in range(ks.size)])
     assert np.max(rel(got.real, acc.real)) < 1e-11
+    # run_random_function_omp: bins sorted over seeds 1..3, k on the reference's log grid
+    import math
+    for i in range(4):
+        kb = 0.5 * math.exp(i * math.log(2.5 / 0.5) / 3)
+        want = sorted(oracle.total_cross_section(3, n, oracle.fill_medium(3, n, s), kb) for s in (1, 2, 3))
+        got = [rfun[3 * i + g] for g in range(3)]
+        assert np.max(rel(np.array(got), np.array(want))) < 1e-10
