@@ -29,6 +29,8 @@ enum { MSGPU_HARDSPHERE = 0, MSGPU_SOFTSPHERE = 1, MSGPU_RESONANT = 2, MSGPU_MAX
 enum { MSGPU_CUBE = 0, MSGPU_BALL = 1, MSGPU_LATTICE = 2, MSGPU_GAUSSIAN = 3 };
 /* Arithmetic of the LU */
 enum { MSGPU_FP64 = 0, MSGPU_MIXED = 1 };
+/* Root methods of the eigenstate search, enum order of reference src/core/eigenstate_list_type.h:20 */
+enum { MSGPU_EIG_DETERMINANT = 0, MSGPU_EIG_MINEIGVAL = 1, MSGPU_EIG_INVTRACEINV = 2 };
 /* Random functions, enum order of reference src/core/random_function_type.h:18 */
 enum { MSGPU_RF_CRSEC = 0, MSGPU_RF_DOS = 1 };
 
@@ -38,6 +40,7 @@ enum { MSGPU_RF_CRSEC = 0, MSGPU_RF_DOS = 1 };
 #define MSGPU_S_NONFINITE 2 /* NaN or Inf reached the result */
 #define MSGPU_S_RANGE 4     /* mixed precision: an entry beyond the FP32-safe range (|M_ij| >= 1e18), no result */
 #define MSGPU_S_TIMEOUT 8   /* a bounded device wait gave up; the result is void */
+#define MSGPU_S_NOCONV 16   /* inverse iteration: not converged within its 50 steps (value = last estimate) */
 
 /* error codes */
 #define MSGPU_E_ARG (-1)
@@ -191,6 +194,31 @@ int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, int nk, const
 int msgpu_random_function(int type, int d, int n, int shape, double ratio, const msgpu_model* model, int nseed,
                           int nbin, double xmin, double xmax, double* data, int* status, int precision);
 
+/* traceinv (src/core/ms_matrix_util.c:319): tr M(k)^-1 per item, by the FP64
+ * engine's n-right-hand-side solve (a MSGPU_MIXED request runs on it too). */
+int msgpu_traceinv_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                         double* out, int* status, int precision);
+/* inverse_iteration (ms_matrix_util.c:279) on M(k) from the constant unit
+ * vector, 50 steps, tolerance 1e-10 (the reference's compute_eigenstates,
+ * ms_core.c:296-312): lambda[2*i] the eigenvalue of smallest modulus, vecs
+ * (may be NULL) the normalised eigenvectors (n complex per item, item order),
+ * status bit MSGPU_S_NOCONV if the iteration did not converge. */
+int msgpu_inverse_iteration_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med,
+                                  const double* ks, double* lambda, double* vecs, int* status, int precision);
+
+/* The root methods "mineigval" and "invtraceinv" (find_eigenstates_serial_2/3,
+ * src/core/ms_core.c:335-401): Muller's method (root_finder.c:342) from each of
+ * the nz starting points z0 (the same for every medium) on the smallest
+ * eigenvalue of M(k) or on 1/tr M(k)^-1; all function values of one step, over
+ * every root and medium, in one batched GPU job.  Non-converged roots dropped,
+ * duplicates (relative 1e-14) removed, order kept: roots[2*(m*nz + i)],
+ * nroots[m]; *nevals (may be NULL) the function evaluations.  mineigval starts
+ * every inverse iteration from the constant unit vector (the reference reuses
+ * the previous call's eigenvector). */
+int msgpu_find_roots_muller_batch(int method, int nmed, const msgpu_medium* media, const double* dom, int nz,
+                                  const double* z0, int maxit, double toler, int precision, double* roots,
+                                  int* nroots, int* nevals);
+
 /* Launch choices (autotuning).  Per (kind, requested precision, size bucket
  * of the job's largest n: (2^(b-1), 2^b]) the engine that runs and the
  * resident CTAs per SM of the persistent grid.  engine: MSGPU_FP64,
@@ -207,7 +235,8 @@ int msgpu_autotune(int kind, int precision, int d, int n, int nitem, double* sec
 
 /* Resident jobs: inputs uploaded once, the hot path run on device-resident
  * data (asynchronously on `stream`, a cudaStream_t or NULL), results fetched
- * separately.  kind: 0 = ln det / n, 1 = dlogf, 2 = amplitudes (as above). */
+ * separately.  kind: 0 = ln det / n, 1 = dlogf, 2 = amplitudes (as above),
+ * 3 = traceinv, 4 = inverse iteration (FP64 engine). */
 typedef struct msgpu_job msgpu_job;
 msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
                             const double* ks, int precision);

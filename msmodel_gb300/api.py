@@ -81,6 +81,11 @@ def lib():
                                              _dp, C.c_void_p, C.c_void_p, C.c_int]
     L.msgpu_random_function.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(_Model), C.c_int,
                                          C.c_int, C.c_double, C.c_double, _dp, _ip, C.c_int]
+    L.msgpu_traceinv_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip, C.c_int]
+    L.msgpu_inverse_iteration_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, C.c_void_p,
+                                                _ip, C.c_int]
+    L.msgpu_find_roots_muller_batch.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), _dp, C.c_int, _dp, C.c_int,
+                                                C.c_double, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
     L.msgpu_tune_set.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.msgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.msgpu_autotune.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
@@ -430,14 +435,84 @@ def solve_aberth_batch(media, dom, z0, nexpsup=4, maxit=30, toler=1e-10, precisi
     return [rc[m, :nr[m]].copy() for m in range(len(media))], ne.value
 
 
-def find_eigenstates(media, dom, ntarget, maxit=30, toler=1e-10, precision="fp64"):
-    """The root search of run_eigenstate_list_serial with method "determinant"
-    (ms_core.c:407-425): ntarget Halton targets sorted by -Im, Aberth with
-    nexpsup = 4, roots finally ordered by -Im (nearest the real axis first)."""
+def traceinv_batch(media, ks, item_med=None, precision="fp64"):
+    """tr M(k)^-1 per item (traceinv, ms_matrix_util.c:319)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    kk, nitem, im = _items(media, ks, item_med)
+    out = np.zeros(2 * nitem)
+    st = np.zeros(nitem, dtype=np.int32)
+    _check(lib().msgpu_traceinv_batch(len(media), _media_array(media), nitem, im, kk, out, st, PRECISION[precision]),
+           "traceinv_batch")
+    return out.view(np.complex128).copy(), st
+
+
+def inverse_iteration_batch(media, ks, item_med=None, want_vecs=True):
+    """inverse_iteration (ms_matrix_util.c:279) on M(k) from the constant unit
+    vector (compute_eigenstates, ms_core.c:296): (lambda, eigenvectors, status)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    kk, nitem, im = _items(media, ks, item_med)
+    lam = np.zeros(2 * nitem)
+    st = np.zeros(nitem, dtype=np.int32)
+    ntot = sum(media[i].n for i in im)
+    vecs = np.zeros(2 * ntot) if want_vecs else None
+    _check(lib().msgpu_inverse_iteration_batch(len(media), _media_array(media), nitem, im, kk, lam,
+                                               None if vecs is None else vecs.ctypes.data, st, 0),
+           "inverse_iteration_batch")
+    parts = None
+    if want_vecs:
+        v = vecs.view(np.complex128)
+        parts, off = [], 0
+        for i in im:
+            parts.append(v[off:off + media[i].n].copy())
+            off += media[i].n
+    return lam.view(np.complex128).copy(), parts, st
+
+
+EIG_METHODS = {"determinant": 0, "mineigval": 1, "invtraceinv": 2}
+
+
+def find_roots_muller(method, media, dom, z0, maxit=30, toler=1e-10, precision="fp64"):
+    """find_eigenstates_serial_2/3 (ms_core.c:335-401) for every medium from the
+    same starting points: (list of root arrays, function evaluations)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    z = _cplx(z0)
+    nz = z.size // 2
+    roots = np.zeros(2 * max(nz, 1) * len(media))
+    nr = np.zeros(len(media), dtype=np.int32)
+    ne = C.c_int(0)
+    _check(lib().msgpu_find_roots_muller_batch(EIG_METHODS[method], len(media), _media_array(media),
+                                               np.asarray(dom, dtype=np.float64), nz, z, maxit, toler,
+                                               PRECISION[precision], roots, nr, C.byref(ne)), "find_roots_muller")
+    r = roots.view(np.complex128)
+    return [r[m * nz:m * nz + nr[m]].copy() for m in range(len(media))], ne.value
+
+
+def find_eigenstates(media, dom, ntarget, maxit=30, toler=1e-10, precision="fp64", method="determinant",
+                     eigenvectors=False):
+    """run_eigenstate_list_serial (ms_core.c:407-435): ntarget Halton targets
+    sorted by -Im, the chosen root method (Aberth with nexpsup = 4 on dlogf for
+    "determinant", Muller for "mineigval" / "invtraceinv"), roots ordered by
+    -Im.  With eigenvectors, also compute_eigenstates (ms_core.c:296): per
+    medium a list of (root, mu, eigenvector) by inverse iteration at each root.
+    Returns (roots per medium, function evaluations[, eigenstates])."""
+    media = [media] if isinstance(media, Medium) else list(media)
     z0 = halton_points(dom, ntarget)
     z0 = z0[np.argsort(-z0.imag, kind="stable")]
-    roots, ne = solve_aberth_batch(media, dom, z0, 4, maxit, toler, precision)
-    return [r[np.argsort(-r.imag, kind="stable")] for r in roots], ne
+    if method == "determinant":
+        roots, ne = solve_aberth_batch(media, dom, z0, 4, maxit, toler, precision)
+    else:
+        roots, ne = find_roots_muller(method, media, dom, z0, maxit, toler, precision)
+    roots = [r[np.argsort(-r.imag, kind="stable")] for r in roots]
+    if not eigenvectors:
+        return roots, ne
+    ks = np.concatenate(roots) if any(len(r) for r in roots) else np.zeros(0, complex)
+    states = [[] for _ in media]
+    if ks.size:
+        im = np.concatenate([np.full(len(r), m, dtype=np.int32) for m, r in enumerate(roots)])
+        lam, vecs, _ = inverse_iteration_batch(media, ks, im)
+        for q in range(ks.size):
+            states[im[q]].append((ks[q], lam[q], vecs[q]))
+    return roots, ne, states
 
 
 # --------------------------------------------------------------------------- autotuning

@@ -27,9 +27,64 @@ namespace msg {
 // right-hand side (kind 2)
 __host__ __device__ inline size_t slot_elems(int kind, size_t slot, int nmax) {
     if (kind == 1) return 2 * slot;
-    // kind 2: the matrix, its copy for the refinement residual (mixed engine), four vectors
-    if (kind == 2) return 2 * slot + 4 * ((((size_t)nmax + 15) / 16) * 16);
+    // kind 2: the matrix, its copy for the refinement residual (mixed engine), four vectors;
+    // kinds 1, 3: the matrix and a right-hand-side matrix; kind 4: the matrix and two vectors
+    const size_t vec = (((size_t)nmax + 15) / 16) * 16;
+    if (kind == 2) return 2 * slot + 4 * vec;
+    if (kind == 1 || kind == 3) return 2 * slot;
+    if (kind == 4) return slot + 2 * vec;
     return slot;
+}
+
+// cnormalize (complex_vector_util.c:47): x /= fac, fac = |x| x_i0/|x_i0| with
+// x_i0 the first nonzero entry (locks the phase); returns fac
+static __device__ zc cnormalize_block(zc* __restrict__ x, int n, LuSmem& s) {
+    double nr = 0.0, z0 = 0.0, z1 = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT) nr += zabs2(x[i]);
+    block_sum3(nr, z0, z1, s);
+    double nzv = -1.0;
+    int nzi = n;
+    for (int i = threadIdx.x; i < n; i += NT)
+        if (x[i].re != 0.0 || x[i].im != 0.0) {
+            nzv = 1.0;
+            nzi = min(nzi, i);
+        }
+    int i0;
+    block_argmax(nzv, nzi, s, i0);
+    if (i0 >= n) return mk(1.0);
+    const zc xi = x[i0];
+    const zc fac = (sqrt(nr) / zabs(xi)) * xi;
+    __syncthreads();  // every thread read x[i0] before it is rescaled
+    const zc rf = 1.0 / fac;
+    for (int i = threadIdx.x; i < n; i += NT) x[i] = x[i] * rf;
+    __syncthreads();
+    return fac;
+}
+
+// inverse_iteration (ms_matrix_util.c:279) on the LU already in A: from the
+// constant unit vector, x <- normalize(A^-1 x) until |x - x_old| < 1e-10 or 50
+// steps (the reference's ivit_maxit / ivit_toler); returns lambda = 1 / fac,
+// the eigenvalue of smallest modulus, x the eigenvector; conv = 0 if not reached.
+static __device__ zc inverse_iteration(const zc* __restrict__ A, zc* __restrict__ x, zc* __restrict__ xold, int n,
+                                       const int* __restrict__ ipiv, LuSmem& s, int& conv) {
+    for (int i = threadIdx.x; i < n; i += NT) x[i] = mk(1.0);
+    __syncthreads();
+    zc fac = cnormalize_block(x, n, s);
+    conv = 0;
+    for (int it = 0; it < 50; ++it) {
+        for (int i = threadIdx.x; i < n; i += NT) xold[i] = x[i];
+        __syncthreads();
+        lu_solve_vec(A, x, n, ipiv, s);
+        fac = cnormalize_block(x, n, s);
+        double d2 = 0.0, z0 = 0.0, z1 = 0.0;
+        for (int i = threadIdx.x; i < n; i += NT) d2 += zabs2(x[i] - xold[i]);
+        block_sum3(d2, z0, z1, s);
+        if (sqrt(d2) < 1e-10) {
+            conv = 1;
+            break;
+        }
+    }
+    return 1.0 / fac;
 }
 
 __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
@@ -52,6 +107,13 @@ __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
         const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
         assemble(A, P.kind == 1 ? B : nullptr, md.n, md.d, md.pos, md.model, k, s);
         zc res;
+        int conv = 1;
+        if (P.kind == 3) {
+            // traceinv (ms_matrix_util.c:319): tr(M^-1 I) by the n-right-hand-side solve
+            for (size_t e = threadIdx.x; e < (size_t)md.n * md.n; e += NT)
+                B[e] = (e % (md.n + 1) == 0) ? mk(1.0) : mk(0.0);
+            __syncthreads();
+        }
         if (P.kind == 2) {
             // incident plane wave along +x (reference incident_wave_util.c:76, ms_core.c:616-618)
             for (int i = threadIdx.x; i < md.n; i += NT) B[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
@@ -60,8 +122,16 @@ __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
         lu_factor(A, md.n, ipiv, s);
         if (P.kind == 0) {
             res = lu_tracelog(A, md.n, ipiv, s);
-        } else if (P.kind == 1) {
+        } else if (P.kind == 1 || P.kind == 3) {
             res = lu_trace_solve(A, B, md.n, ipiv, s);
+        } else if (P.kind == 4) {
+            const size_t vec = (((size_t)P.piv_stride + 15) / 16) * 16;
+            res = inverse_iteration(A, B, B + vec, md.n, ipiv, s, conv);
+            if (P.amps)
+                for (int i = threadIdx.x; i < md.n; i += NT) {
+                    P.amps[2 * (P.amp_off[it] + i)] = B[i].re;
+                    P.amps[2 * (P.amp_off[it] + i) + 1] = B[i].im;
+                }
         } else {
             lu_solve_vec(A, B, md.n, ipiv, s);
             // optical theorem sigma = -Im(conj(phi).a)/k (reference ms_matrix_util.c:361)
@@ -85,6 +155,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
             int st = 0;
             if (s.info) st |= MSGPU_S_SINGULAR;
             if (!isfinite(res.re) || !isfinite(res.im)) st |= MSGPU_S_NONFINITE;
+            if (!conv) st |= MSGPU_S_NOCONV;
             P.status[it] = st;
         }
         __syncthreads();
@@ -449,17 +520,21 @@ static int set_items_locked(msgpu_job* J, int nitem, const int* item_med, const 
         if (mi < 0 || mi >= J->nmed) return set_err(MSGPU_E_ARG, "job: bad item medium");
         med_of[i] = mi;
         const double n = J->med_n[mi], n3 = n * n * n, n2 = n * n;
-        flops += (J->kind == 0) ? 8.0 / 3.0 * n3 : (J->kind == 1 ? (8.0 / 3.0 + 8.0) * n3 : 8.0 / 3.0 * n3 + 8.0 * n2);
+        flops += (J->kind == 0) ? 8.0 / 3.0 * n3
+                 : (J->kind == 1 || J->kind == 3) ? (8.0 / 3.0 + 8.0) * n3
+                 : (J->kind == 2) ? 8.0 / 3.0 * n3 + 8.0 * n2
+                                  : 8.0 / 3.0 * n3 + 50 * 8.0 * n2;  // kind 4: at most 50 solves
         amp_total += J->med_n[mi];
     }
-    if (J->kind == 2 && J->d_amps && amp_total > J->amp_cap) return set_err(MSGPU_E_SIZE, "job: amplitudes exceed capacity");
+    if ((J->kind == 2 || J->kind == 4) && J->d_amps && amp_total > J->amp_cap)
+        return set_err(MSGPU_E_SIZE, "job: amplitudes exceed capacity");
     std::vector<int> order(nitem);
     for (int i = 0; i < nitem; i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return J->med_n[med_of[a]] > J->med_n[med_of[b]]; });
     CK(cudaMemcpy(J->d_ks, ks, sizeof(double) * 2 * nitem, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(J->d_item_med, med_of.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(J->d_order, order.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice));
-    if (J->kind == 2 && J->d_amp_off) {
+    if ((J->kind == 2 || J->kind == 4) && J->d_amp_off) {
         std::vector<long long> off(nitem);
         long long acc = 0;
         for (int i = 0; i < nitem; i++) { off[i] = acc; acc += J->med_n[med_of[i]]; }
@@ -477,7 +552,7 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
                             const double* ks, int precision) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (init_locked(-1)) return nullptr;
-    if (kind < 0 || kind > 2 || nmed < 1 || !media || nitem < 1 || !ks) {
+    if (kind < 0 || kind > 4 || nmed < 1 || !media || nitem < 1 || !ks) {
         set_err(MSGPU_E_ARG, "job: bad argument");
         return nullptr;
     }
@@ -487,7 +562,7 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     }
     auto* J = new msgpu_job();
     J->kind = kind;
-    J->precision = precision;
+    J->precision = kind >= 3 ? MSGPU_FP64 : precision;  // traceinv, inverse iteration: FP64 engine
     J->cap = nitem;
     J->nmed = nmed;
     J->med_n.resize(nmed);
@@ -519,8 +594,8 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     if (cudaMalloc(&J->d_status, sizeof(int) * nitem) != cudaSuccess) return fail("alloc status");
     if (cudaMalloc(&J->d_counter, 256) != cudaSuccess) return fail("alloc counter");
     if (cudaMemset(J->d_counter, 0, 256) != cudaSuccess) return fail("clear counter");
-    if (kind == 2) {
-        // capacity for the amplitudes of nitem items of the largest medium
+    if (kind == 2 || kind == 4) {
+        // capacity for the amplitudes (eigenvectors) of nitem items of the largest medium
         J->amp_cap = (long long)nitem * J->nmax;
         if (cudaMalloc(&J->d_amps, sizeof(double) * 2 * (size_t)J->amp_cap) != cudaSuccess) return fail("alloc amps");
         if (cudaMalloc(&J->d_amp_off, sizeof(long long) * nitem) != cudaSuccess) return fail("alloc amp_off");
@@ -543,7 +618,7 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     // per-CTA slots
     J->slot = (size_t)J->nmax * J->nmax;
     const size_t per_cta = slot_elems(kind, J->slot, J->nmax) * sizeof(zc);
-    const TuneEntry& te = g_tune[kind][precision][size_bucket(J->nmax)];
+    const TuneEntry te = kind < 3 ? g_tune[kind][precision][size_bucket(J->nmax)] : TuneEntry{};
     if (te.engine) J->precision = te.engine - 1;
     const int ctas = te.ctas ? std::min(te.ctas, g_ctas_fp64) : g_ctas_fp64;
     int grid = std::min(nitem, g_sms * ctas);
@@ -653,7 +728,8 @@ int msgpu_job_results(msgpu_job* J, double* out, int* status) {
 }
 
 int msgpu_job_amplitudes(msgpu_job* J, double* amps) {
-    if (!J || J->kind != 2 || !amps) return set_err(MSGPU_E_ARG, "job_amplitudes: not an amplitude job");
+    if (!J || (J->kind != 2 && J->kind != 4) || !amps)
+        return set_err(MSGPU_E_ARG, "job_amplitudes: not an amplitude or eigenvector job");
     CK(cudaDeviceSynchronize());
     CK(cudaMemcpy(amps, J->d_amps, sizeof(double) * 2 * (size_t)J->amp_total, cudaMemcpyDeviceToHost));
     return 0;
@@ -774,6 +850,22 @@ int msgpu_tracelog_batch(int nmed, const msgpu_medium* media, int nitem, const i
 int msgpu_dk_log_det_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
                            double* out, int* status, int precision) {
     return run_batch(1, nmed, media, nitem, item_med, ks, out, status, precision);
+}
+
+int msgpu_traceinv_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                         double* out, int* status, int precision) {
+    return run_batch(3, nmed, media, nitem, item_med, ks, out, status, precision);
+}
+
+int msgpu_inverse_iteration_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med,
+                                  const double* ks, double* lambda, double* vecs, int* status, int precision) {
+    msgpu_job* J = msgpu_job_create(4, nmed, media, nitem, item_med, ks, precision);
+    if (!J) return MSGPU_E_ARG;
+    int e = msgpu_job_run(J, nullptr);
+    if (!e) e = msgpu_job_results(J, lambda, status);
+    if (!e && vecs) e = msgpu_job_amplitudes(J, vecs);
+    msgpu_job_destroy(J);
+    return e;
 }
 
 int msgpu_amplitude_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,

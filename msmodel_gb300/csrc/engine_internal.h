@@ -26,8 +26,8 @@ struct EngineParams {
     double* out;          // 2 * nitem
     int* status;          // nitem
     unsigned* counter;    // [0] work queue; [1] live items (queue positions >= it are past the end)
-    int kind;             // 0 ln det / n, 1 dlogf, 2 amplitudes a = M^-1 phi
-    double* amps;         // kind 2: a per item (2 * n_i doubles each) or nullptr
+    int kind;             // 0 ln det / n, 1 dlogf, 2 amplitudes a = M^-1 phi, 3 traceinv, 4 inverse iteration
+    double* amps;         // kinds 2, 4: a (or the eigenvector) per item (2 * n_i doubles each) or nullptr
     const long long* amp_off;  // kind 2: offset (in complex elements) of item i in amps
 };
 

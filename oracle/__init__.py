@@ -239,6 +239,9 @@ class Reference:
         L.ref_wavefunction.argtypes = med + [_dp, C.c_int, C.c_int, _dp, _dp, _dp]
         L.ref_save_cdata.argtypes = [C.c_int, _dp, C.c_char_p]
         L.ref_parse_cdata.argtypes = [C.c_int, C.c_char_p, _dp]
+        L.ref_traceinv.argtypes = med + [C.c_int, _dp, _dp]
+        L.ref_inverse_iteration.argtypes = med + [_dp, _dp, _dp]
+        L.ref_roots_muller.argtypes = [C.c_int] + med + [_dp, C.c_int, _dp, C.c_int, C.c_double]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
 
     @staticmethod
@@ -286,6 +289,27 @@ class Reference:
 
     def total_cross_section(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
         return self.L.ref_total_cross_section(*self._med(d, n, model, params, shape, ratio, seed), float(k))
+
+    def traceinv(self, d, n, seed, ks, model="maximum", params=(), shape="ball", ratio=1.0):
+        kk = _cplx_array(ks)
+        out = np.zeros_like(kk)
+        self.L.ref_traceinv(*self._med(d, n, model, params, shape, ratio, seed), kk.size // 2, kk, out)
+        return out.view(np.complex128).copy()
+
+    def inverse_iteration(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
+        lam = np.zeros(2)
+        vec = np.zeros(2 * n)
+        conv = self.L.ref_inverse_iteration(*self._med(d, n, model, params, shape, ratio, seed),
+                                            np.array([k.real, k.imag]), lam, vec)
+        return complex(lam[0], lam[1]), vec.view(np.complex128).copy(), conv
+
+    def roots_muller(self, method, d, n, seed, dom, z0, maxit=30, toler=1e-10, model="maximum", params=(),
+                     shape="ball", ratio=1.0):
+        z = _cplx_array(z0)
+        nr = self.L.ref_roots_muller({"mineigval": 1, "invtraceinv": 2}[method],
+                                     *self._med(d, n, model, params, shape, ratio, seed),
+                                     np.asarray(dom, dtype=float), z.size // 2, z, maxit, toler)
+        return z.view(np.complex128)[:nr].copy()
 
     def save_cdata(self, values, fname):
         z = np.ascontiguousarray(np.asarray(values, dtype=np.complex128))

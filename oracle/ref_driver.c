@@ -15,6 +15,7 @@
 #include "green_bessel.h"
 #include "ms_matrix_util.h"
 #include "root_finder.h"
+#include "complex_vector_util.h"
 #include "real_vector_util.h"
 #include "complex_data_type.h"
 #include "complex_data_util.h"
@@ -189,4 +190,79 @@ void ref_parse_cdata(int n, const char* text, double* data) {
     char* copy = strdup(text);
     parse_cdata(&cd, copy);
     free(copy);
+}
+
+/* traceinv (ms_matrix_util.c:319) of M(k) */
+void ref_traceinv(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+                  int nk, const double* ks, double* out) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    dcomplex* a = (dcomplex*)malloc(sizeof(dcomplex) * (size_t)n * n);
+    for (int l = 0; l < nk; l++) {
+        build_ms_matrix(&med, ks[2 * l] + I * ks[2 * l + 1], a);
+        dcomplex t = traceinv(n, a);
+        out[2 * l] = creal(t); out[2 * l + 1] = cimag(t);
+    }
+    free(a);
+    drop_medium(&med);
+}
+
+/* compute_eigenstates' step (ms_core.c:302-308): inverse_iteration of M(k)
+ * from the constant unit vector, 50 steps, 1e-10; returns the convergence flag */
+int ref_inverse_iteration(int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                          unsigned long seed, const double* k, double* lambda, double* vec) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    dcomplex* a = (dcomplex*)malloc(sizeof(dcomplex) * (size_t)n * n);
+    build_ms_matrix(&med, k[0] + I * k[1], a);
+    constant_unit_cvector(n, (dcomplex*)vec);
+    dcomplex mu;
+    int conv = inverse_iteration(n, a, (dcomplex*)vec, &mu, 50, 1e-10, 0);
+    lambda[0] = creal(mu); lambda[1] = cimag(mu);
+    free(a);
+    drop_medium(&med);
+    return conv;
+}
+
+/* find_eigenstates_serial_2 / _3 (ms_core.c:335-401): Muller on the smallest
+ * eigenvalue (method 1; one eigenvector shared by all calls, as the reference)
+ * or on 1/traceinv (method 2), then filter_cvector and uniq_cvector(1e-14) */
+static int g_n;
+static dcomplex *g_mat, *g_vec;
+static dcomplex g_mineigval(dcomplex k) {
+    dcomplex mu;
+    build_ms_matrix(g_med, k, g_mat);
+    inverse_iteration(g_n, g_mat, g_vec, &mu, 50, 1e-10, 0);
+    return mu;
+}
+static dcomplex g_invtrinv(dcomplex k) {
+    build_ms_matrix(g_med, k, g_mat);
+    return 1. / traceinv(g_n, g_mat);
+}
+int ref_roots_muller(int method, int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                     unsigned long seed, const double* dom, int nz, double* z, int maxit, double toler) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    Domain dm = {dom[0], dom[1], dom[2], dom[3]};
+    g_med = &med;
+    g_n = n;
+    g_mat = (dcomplex*)calloc((size_t)n * n, sizeof(dcomplex));
+    g_vec = (dcomplex*)calloc((size_t)n, sizeof(dcomplex));
+    constant_unit_cvector(n, g_vec);
+    int* conv = (int*)calloc((size_t)nz, sizeof(int));
+    dcomplex* kr = (dcomplex*)z;
+    for (int i = 0; i < nz; i++) {
+        if (method == 1) {
+            conv[i] = find_root_muller(g_mineigval, &dm, &kr[i], maxit, toler, 0);
+            conv[i] *= (cabs(g_mineigval(kr[i])) < sqrt(toler));
+        } else {
+            conv[i] = find_root_muller(g_invtrinv, &dm, &kr[i], maxit, toler, 0);
+        }
+    }
+    int nroot = nz;
+    filter_cvector(&nroot, kr, conv);
+    uniq_cvector(&nroot, kr, 1e-14);
+    free(conv); free(g_mat); free(g_vec);
+    drop_medium(&med);
+    return nroot;
 }

@@ -146,6 +146,21 @@ def reference_runs():
     # total cross section (zgesv path)
     for k in (0.5, 2.0):
         add("total_cross_section", d=3, n=120, seed=9, k=k, out=r.total_cross_section(3, 120, 9, k))
+    # traceinv, inverse iteration (compute_eigenstates) and the Muller root methods
+    kk = [1.1 - 0.1j, 2.3 - 0.02j, 0.7 - 0.4j]
+    add("traceinv", d=3, n=80, seed=2, ks=_cl(kk), out=_cl(r.traceinv(3, 80, 2, kk)))
+    ab = [c for c in runs["cases"] if c["kind"] == "aberth" and c["n"] == 100][0]
+    for k in [complex(*ab["roots"][0]), complex(*ab["roots"][3]), 1.7 - 0.2j]:
+        lam, vec, conv = r.inverse_iteration(3, 100, 1, k)
+        add("inverse_iteration", d=3, n=100, seed=1, k=[k.real, k.imag], lam=[lam.real, lam.imag],
+            vec=_cl(vec), conv=int(conv))
+    dom = [0.5, 3.0, -1.0, 0.0]
+    z0 = o.halton_points(dom, 12)
+    z0 = z0[np.argsort(-z0.imag, kind="stable")]
+    for method in ("invtraceinv", "mineigval"):
+        roots = r.roots_muller(method, 3, 100, 1, dom, z0, maxit=30, toler=1e-10)
+        add("roots_muller", method=method, d=3, n=100, seed=1, dom=dom, z0=_cl(z0), maxit=30, toler=1e-10,
+            roots=_cl(roots))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
