@@ -248,6 +248,13 @@ __device__ __forceinline__ void issue_tile_mmas(MixSmem& s, uint32_t tmem) {
     umma_commit(&s.bar_mma);
 }
 
+__device__ __forceinline__ df df_sub_levels(df c, float l0, float l1, float l23) {
+    const df s = two_sum(c.h, -l0);
+    const df t = two_sum(s.h, -l1);
+    const float lo = __fsub_rn(__fadd_rn(__fadd_rn(s.l, t.l), c.l), l23);
+    return quick_two_sum(t.h, lo);
+}
+
 // C[m x nn] -= Ap[m x K] * Bp[K x nn]; all double-float complex, column-major.
 // tri != 0: only tiles holding an element with row >= column are updated.
 // Returns false if a wait timed out (the engine then stops).
@@ -343,11 +350,11 @@ __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __
                         const float sc = ldexpf(1.0f, ea_r + __ldg(geb + col) - 16);
                         const float4 cv = cpre[cc + j];
                         dfc c = dfc{df{cv.x, cv.y}, df{cv.z, cv.w}};
-                        // level 0 + level 1 is exact as a double-float; level 2+3 added with rounding
-                        const df vr = df_add(two_sum(g[0][j] * sc, g[2][j] * sc), df{g[4][j] * sc, 0.0f});
-                        const df vi = df_add(two_sum(g[1][j] * sc, g[3][j] * sc), df{g[5][j] * sc, 0.0f});
-                        c.re = df_sub(c.re, vr);
-                        c.im = df_sub(c.im, vi);
+                        // c - (L0 + L1 + L23) sc: level 0 and level 1 enter exactly (integers
+                        // times a power of two, two-sums), level 2+3 and every error term in one
+                        // FP32 accumulator, one renormalisation per component
+                        c.re = df_sub_levels(c.re, g[0][j] * sc, g[2][j] * sc, g[4][j] * sc);
+                        c.im = df_sub_levels(c.im, g[1][j] * sc, g[3][j] * sc, g[5][j] * sc);
                         dfc_store(C + row + (size_t)col * ldc, c);
                     }
                 }
