@@ -44,8 +44,6 @@ int mixed_run(const EngineParams& P, int grid, int nmax, bool d3only, cudaStream
 int mixed_prepare(int grid, int nmax);
 // Changes whenever the mixed engine's scratch is reallocated (captured graphs hold its address).
 unsigned long long mixed_generation();
-// kernels launched by the mixed engine for one run
-int mixed_launches();
 // per-phase SM cycles of the last mixed run made with MSGPU_STATS set:
 // assemble, panel, trsm, slice, tiles, solve, items
 int mixed_stats(double* out, int n);

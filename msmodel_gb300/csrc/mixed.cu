@@ -1,6 +1,8 @@
 // mixed.cu -- mixed-precision engine: the LU trailing updates run on the
 // tcgen05 tensor cores as exact products of bf16 slices, everything else in
-// double-float (FP32 hi + lo) on the FP32 pipe, assembly and ln in FP64.
+// double-float (FP32 hi + lo) on the FP32 pipe: the panel, the TRSM, the
+// epilogue and, for d = 3, the whole matrix assembly; the pivot reciprocals,
+// ln and the d = 2 Green functions (K_nu) in FP64.
 //
 // Trailing update C -= A B (A: m x K panel, B: K x nn rows, K <= 32, complex):
 //  * every row of A (column of B) is scaled by a power of two so its largest
@@ -15,7 +17,8 @@
 //    Foldy-Lax matrices (d = 3, N <= 1024, Im k >= -1; d = 2 with moderate
 //    Im k) put ln det within ~3e-9 of FP64 with 4 slices; entries spanning
 //    more than ~1e5 within a row (d = 2 far below the real axis) lose
-//    accuracy (about 1e-7), since the scale is per row;
+//    accuracy (up to ~1e-5 at d = 2, N = 2048, Im k = -0.3), since the
+//    scale is per row;
 //  * complex = 4 real products, Re uses the negate-B bit of the instruction
 //    descriptor: 40 tcgen05.mma (128 x 32 x 16) per K-step into six TMEM
 //    accumulators (3 levels x Re/Im, 192 columns);
@@ -767,44 +770,44 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                 mx = assemble_tile_grouped(A, B, n, d, pos, k, I, J, dg0, dg1, s, mx);
             } else {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
-                const int i = I * 32 + ii, j = J * 32 + jj;
-                if (i < n && j < n && i <= j) {
-                    float4 fm, fd = make_float4(0, 0, 0, 0);
-                    if (i < j && d3) {
-                        // the whole element on the FP32 pipe in double-float (green_df.cuh)
-                        const float4 pa = s.u.p.ci[ii], pb = s.u.p.cj[jj];
-                        const float2 za = s.u.p.ciz[ii], zb = s.u.p.cjz[jj];
-                        const df ex = df_sub(df{pa.x, pa.y}, df{pb.x, pb.y});
-                        const df ey = df_sub(df{pa.z, pa.w}, df{pb.z, pb.w});
-                        const df ez = df_sub(df{za.x, za.y}, df{zb.x, zb.y});
-                        const df r = df_sqrt(df_add(df_add(df_mul(ex, ex), df_mul(ey, ey)), df_mul(ez, ez)));
-                        dfc a, b;
-                        pair_elements_df3t(s.u.p.tab, kr, ki, grow, r, B != nullptr, a, b);
-                        fm = make_float4(a.re.h, a.re.l, a.im.h, a.im.l);
-                        if (B) fd = make_float4(b.re.h, b.re.l, b.im.h, b.im.l);
-                    } else {
-                        zc m, dm = mk(0.0);
-                        if (i < j) {
-                            pair_elements(d, k, atom_distance(d, pos, i, j), B != nullptr, m, dm);
+                for (int q = 0; q < 4; ++q) {
+                    const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+                    const int i = I * 32 + ii, j = J * 32 + jj;
+                    if (i < n && j < n && i <= j) {
+                        float4 fm, fd = make_float4(0, 0, 0, 0);
+                        if (i < j && d3) {
+                            // the whole element on the FP32 pipe in double-float (green_df.cuh)
+                            const float4 pa = s.u.p.ci[ii], pb = s.u.p.cj[jj];
+                            const float2 za = s.u.p.ciz[ii], zb = s.u.p.cjz[jj];
+                            const df ex = df_sub(df{pa.x, pa.y}, df{pb.x, pb.y});
+                            const df ey = df_sub(df{pa.z, pa.w}, df{pb.z, pb.w});
+                            const df ez = df_sub(df{za.x, za.y}, df{zb.x, zb.y});
+                            const df r = df_sqrt(df_add(df_add(df_mul(ex, ex), df_mul(ey, ey)), df_mul(ez, ez)));
+                            dfc a, b;
+                            pair_elements_df3t(s.u.p.tab, kr, ki, grow, r, B != nullptr, a, b);
+                            fm = make_float4(a.re.h, a.re.l, a.im.h, a.im.l);
+                            if (B) fd = make_float4(b.re.h, b.re.l, b.im.h, b.im.l);
                         } else {
-                            m = dg0;
-                            dm = dg1;
+                            zc m, dm = mk(0.0);
+                            if (i < j) {
+                                pair_elements(d, k, atom_distance(d, pos, i, j), B != nullptr, m, dm);
+                            } else {
+                                m = dg0;
+                                dm = dg1;
+                            }
+                            fm = cvt(m);
+                            if (B) fd = cvt(dm);
                         }
-                        fm = cvt(m);
-                        if (B) fd = cvt(dm);
-                    }
-                    mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
-                    A[i + (size_t)j * n] = fm;
-                    s.u.p.T[jj][ii] = fm;
-                    if (B) {
-                        mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
-                        B[i + (size_t)j * n] = fd;
-                        s.u.p.T2[jj][ii] = fd;
+                        mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                        A[i + (size_t)j * n] = fm;
+                        s.u.p.T[jj][ii] = fm;
+                        if (B) {
+                            mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                            B[i + (size_t)j * n] = fd;
+                            s.u.p.T2[jj][ii] = fd;
+                        }
                     }
                 }
-            }
             }
             __syncthreads();
 #pragma unroll
@@ -1109,7 +1112,6 @@ uint8_t* g_img = nullptr;
 size_t g_img_bytes = 0;
 int* g_err = nullptr;
 unsigned long long* g_stats = nullptr;
-int g_launches_last = 0;
 }  // namespace
 
 static size_t mixed_smem() { return sizeof(MixSmem) + 1024; }
@@ -1186,11 +1188,8 @@ int mixed_run(const EngineParams& P, int grid, int nmax, bool d3only, cudaStream
         else if (P.kind == 1) k_engine_mixed<1, false><<<grid, NT, sm, st>>>(P, X);
         else k_engine_mixed<2, false><<<grid, NT, sm, st>>>(P, X);
     }
-    g_launches_last = 1;
     return cudaGetLastError() == cudaSuccess ? 0 : MSGPU_E_CUDA;
 }
-
-int mixed_launches() { return g_launches_last; }
 
 int mixed_stats(double* out, int n) {
     if (!g_stats) return 0;
