@@ -9,7 +9,17 @@ sample = 4096).  One step = the hot path over the whole cut.
   value  : evals/s with positions and k already resident in HBM (msgpu_job_run)
   e2e    : evals/s through the C-ABI call a user makes with host buffers
            (msgpu_tracelog_batch: H2D of inputs, the kernels, D2H of results)
-  roofline, cpu_baseline, clocks, gpu_launches as documented in DESIGN.md.
+  roofline: the engine's binding unit (the FP64 pipe, peak = a DFMA probe run
+           here) with achieved = 8/3 N^3 flops per ln det / step time, and
+           the DRAM traffic of one ncu capture scaled to the launch
+  cpu_baseline: the reference algorithm on all host cores, bounded sample
+  clocks: nvidia-smi samples during the timed region
+  gpu_launches: this library's kernel launches in the timed region
+  mixed / aberth: the mixed-precision engine on the same cut, and the
+           resonance search (FP64 and mixed) over 32 realisations
+
+Other configurations print one line each with --workload map64 | map2d |
+aberth | wave.
 
 Multi-GPU (torchrun): weak scaling -- each rank evaluates the full cut for its
 own realisation (seed = rank + 1); no collective on the data path.
