@@ -162,47 +162,9 @@ __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
     }
 }
 
-// single-matrix kernels used by the drop-in layer ---------------------------------
+// single-matrix assembly for the drop-in layer (build_matrix.cu)
 __global__ void __launch_bounds__(NT, 1) k_build_matrix(zc* A, int n, int d, const double* pos, msgpu_model m,
-                                                        double kre, double kim, int deriv) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    LuSmem& s = *reinterpret_cast<LuSmem*>(smem_raw);
-    // a grid of CTAs shares the column tiles: CTA b assembles column tiles J = b, b + grid, ...
-    const int tid = threadIdx.x;
-    const zc k = mk(kre, kim);
-    if (tid == 0) s.diag[0] = deriv ? dk_invf(m, d, k) : invf(m, d, k);
-    __syncthreads();
-    const int nt = (n + 31) / 32;
-    for (int J = blockIdx.x; J < nt; J += gridDim.x) {
-        for (int I = 0; I <= J; ++I) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
-                const int i = I * 32 + ii, j = J * 32 + jj;
-                if (i < n && j < n && i <= j) {
-                    zc v;
-                    if (i < j) {
-                        zc mm, dm;
-                        pair_elements(d, k, atom_distance(d, pos, i, j), deriv != 0, mm, dm);
-                        v = deriv ? dm : mm;
-                    } else {
-                        v = s.diag[0];
-                    }
-                    A[i + (size_t)j * n] = v;
-                    s.T[jj][ii] = v;
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int jj = tid & 31, ii = (tid >> 5) + 8 * q;
-                const int i = I * 32 + ii, j = J * 32 + jj;
-                if (j < n && i < j) A[j + (size_t)i * n] = s.T[jj][ii];
-            }
-            __syncthreads();
-        }
-    }
-}
+                                                        double kre, double kim, int deriv);
 
 __global__ void __launch_bounds__(NT, 1) k_tracelog_matrix(zc* A, int n, int* ipiv, double* out, int* info) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -218,45 +180,9 @@ __global__ void __launch_bounds__(NT, 1) k_tracelog_matrix(zc* A, int n, int* ip
     }
 }
 
+// device special functions for the checks against the reference goldens (special.cu)
 __global__ void k_eval_special(int which, int d, msgpu_model m, int n, const double* ks, const double* rs,
-                               double* out) {
-    __shared__ Df3Tables tab;
-    if (which >= 7) {  // block-uniform
-        df3_tables_init(tab);
-        __syncthreads();
-    }
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    zc k = mk(ks[2 * i], ks[2 * i + 1]);
-    double r = rs ? rs[i] : 1.0;
-    zc v;
-    switch (which) {
-    case 0: v = free_green(d, k, r); break;
-    case 1: v = dk_free_green(d, k, r); break;
-    case 2: v = free_green_imag(d, k, r); break;
-    case 3: v = bessel_k(d, k); break;
-    case 5:
-    case 6: {  // d = 3 matrix elements as the mixed engine evaluates them (double-float)
-        dfc a, b;
-        pair_elements_df3(k, r, which == 6, a, b);
-        const dfc e = which == 5 ? a : b;
-        v = mk(df_to_double(e.re), df_to_double(e.im));
-        break;
-    }
-    case 7:
-    case 8: {  // the same elements entirely on the FP32 pipe, as the mixed engine assembles them
-        dfc a, b;
-        pair_elements_df3t(tab, df_from_double(k.re), df_from_double(k.im), k.im != 0.0, df_from_double(r),
-                           which == 8, a, b);
-        const dfc e = which == 7 ? a : b;
-        v = mk(df_to_double(e.re), df_to_double(e.im));
-        break;
-    }
-    default: v = invf(m, d, k); break;
-    }
-    out[2 * i] = v.re;
-    out[2 * i + 1] = v.im;
-}
+                               double* out);
 
 // FP64 FMA throughput probe: 8 independent chains per thread; the roofline
 // denominator of the plain (FP64-pipe-bound) path.
