@@ -134,8 +134,8 @@ def cpu_baseline(seconds=15.0, nk_cap=NK):
         el = time.perf_counter() - t0
         if el >= seconds and i >= 2:
             break
-    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmsref.so")) and False else "port"
-    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": kind,
+    # the oracle port: the reference's compiled sources are not on the GPU host
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"first {done} of the 4096 cut points, N=1024 d=3 seed 1, {threads} OpenMP threads x "
                       f"1 OpenBLAS thread ({o.lapack_config().split()[0:2]})", "seconds": el}
 
