@@ -191,6 +191,9 @@ def measure_mixed(ms, torch, med, ks, out64, args, stream, flush, ws, barrier):
                          "peak": read_peaks().get("bf16_tflops_sustained", 1728.6), "unit": "TFLOP/s",
                          "frac": tensor_flops / 1e12 / read_peaks().get("bf16_tflops_sustained", 1728.6),
                          "counted": "bf16 tensor flops executed (80/3 n^3 per ln det)",
+                         "observed": "not tensor-bound: ncu at N=512 (profiles/k_engine_mixed_kcut_n512.md) shows "
+                                     "FP32 pipe 26%, tensor 3.7%, FP64 4%, DRAM 29% of peak, stalls on global "
+                                     "memory and barriers (double-float panel, TRSM, trailing-matrix round trips)",
                          "algorithmic_tflops": 8.0 / 3.0 * n ** 3 * len(ks) / (tot / args.steps) / 1e12}}
 
 
