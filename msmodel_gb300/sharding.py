@@ -48,3 +48,51 @@ def run_tracelog_sharded(d, n, ks, nseed, rank, world, compute=None, gather=None
         allv.update(p)
     assert sorted(allv) == list(range(1, nseed + 1)), "missing seeds after gather"
     return seed_average([allv[s] for s in range(1, nseed + 1)])
+
+
+def deal_by_cost(costs, world):
+    """Indices dealt to `world` ranks, largest cost first, each to the rank with
+    the least work so far (ties to the lowest rank): the uneven realisation
+    sizes of the batched resonance search balance without any exchange."""
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(costs)), key=lambda i: (-costs[i], i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
+def run_aberth_sharded(sizes, rank, world, compute=None, gather=None, dom=(0.5, 3.0, -1.0, 0.0), ntarget=32,
+                       nbin=40, precision="mixed"):
+    """The batched resonance search over realisations r = 1..len(sizes) (n_r =
+    sizes[r-1], positions from fill_medium(seed=r)), split over `world` ranks by
+    n^3 cost.  Each rank searches its own realisations on its GPU; one gather
+    then joins the variable-length root lists and adds the ranks' histograms
+    of Im k (nbin bins on [dom[2], dom[3]]).
+
+    compute(list of realisation indices r) -> {r: roots}; defaults to this
+    rank's GPU (find_eigenstates, method "determinant").
+    gather(obj) -> list of every rank's obj (e.g. torch.distributed.all_gather_object).
+    Returns ({r: roots} for every realisation, histogram counts)."""
+    mine = deal_by_cost([float(n) ** 3 for n in sizes], world)[rank]
+    reals = [i + 1 for i in mine]
+    if compute is None:
+        from . import api
+
+        def compute(rs):
+            if not rs:
+                return {}
+            media = [api.Medium(3, sizes[r - 1], seed=r) for r in rs]
+            roots, _ = api.find_eigenstates(media, list(dom), ntarget, precision=precision)
+            return dict(zip(rs, roots))
+    roots = compute(reals)
+    allr = np.concatenate([np.asarray(v) for v in roots.values()]) if roots else np.zeros(0, complex)
+    hist, _ = np.histogram(allr.imag, bins=nbin, range=(dom[2], dom[3]))
+    parts = gather((roots, hist)) if gather is not None else [(roots, hist)]
+    every, total = {}, np.zeros(nbin, dtype=np.int64)
+    for r_part, h_part in parts:
+        every.update(r_part)
+        total += h_part
+    assert sorted(every) == list(range(1, len(sizes) + 1)), "missing realisations after gather"
+    return every, total
