@@ -219,6 +219,14 @@ int msgpu_find_roots_muller_batch(int method, int nmed, const msgpu_medium* medi
                                   const double* z0, int maxit, double toler, int precision, double* roots,
                                   int* nroots, int* nevals);
 
+/* The eigenvalues mu of M(k) per item (eigvals, src/core/ms_matrix_util.c:147,
+ * the input of the mu-plane histograms, ms_core.c:173-282): M(k) assembled on
+ * the GPU, the general complex eigenproblem solved by cuSOLVER (Xgeev, no
+ * eigenvectors).  mu receives n complex values per item, items in order;
+ * status (may be NULL) MSGPU_S_NOCONV where the QR iteration did not converge. */
+int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
+                        double* mu, int* status);
+
 /* Launch choices (autotuning).  Per (kind, requested precision, size bucket
  * of the job's largest n: (2^(b-1), 2^b]) the engine that runs and the
  * resident CTAs per SM of the persistent grid.  engine: MSGPU_FP64,

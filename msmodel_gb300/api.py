@@ -86,6 +86,7 @@ def lib():
                                                 _ip, C.c_int]
     L.msgpu_find_roots_muller_batch.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), _dp, C.c_int, _dp, C.c_int,
                                                 C.c_double, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
+    L.msgpu_eigvals_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip]
     L.msgpu_tune_set.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.msgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.msgpu_autotune.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
@@ -466,6 +467,44 @@ def inverse_iteration_batch(media, ks, item_med=None, want_vecs=True):
             parts.append(v[off:off + media[i].n].copy())
             off += media[i].n
     return lam.view(np.complex128).copy(), parts, st
+
+
+def eigvals_batch(media, ks, item_med=None):
+    """The n eigenvalues of M(k) per item (eigvals, ms_matrix_util.c:147):
+    (list of arrays, status)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    kk, nitem, im = _items(media, ks, item_med)
+    mu = np.zeros(2 * sum(media[i].n for i in im))
+    st = np.zeros(nitem, dtype=np.int32)
+    _check(lib().msgpu_eigvals_batch(len(media), _media_array(media), nitem, im, kk, mu, st), "eigvals_batch")
+    mu = mu.view(np.complex128)
+    out, off = [], 0
+    for i in im:
+        out.append(mu[off:off + media[i].n].copy())
+        off += media[i].n
+    return out, st
+
+
+def imag_mu_histogram(mus, nbin, xmin, xmax):
+    """Histogram of Im mu on log-spaced bins over [xmin, xmax] (0 < xmin), as
+    run_imag_mu_histogram_omp builds it (imag_mu_histogram_util.c:108-153):
+    bin floor(nbin (ln Im mu - ln xmin) / ln(xmax/xmin)), samples outside the
+    range lost, then normalised to unit integral (each bin divided by its
+    width, total * x_centre * ln(xmax/xmin)/nbin).  Returns (density, bin
+    centres, lost count)."""
+    x = np.concatenate([np.asarray(m).imag for m in mus])
+    counts = np.zeros(nbin)
+    lost = 0
+    lo, hi = np.log(xmin), np.log(xmax)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        idx = np.floor(nbin * (np.log(x) - lo) / (hi - lo))
+    ok = np.isfinite(idx) & (idx >= 0) & (idx < nbin)
+    np.add.at(counts, idx[ok].astype(int), 1.0)
+    lost = int(x.size - ok.sum())
+    centres = xmin * np.exp(np.log(xmax / xmin) * (np.arange(nbin) + 0.5) / nbin)
+    total = counts.sum()
+    dens = counts / (centres * total * np.log(xmax / xmin) / nbin) if total else counts
+    return dens, centres, lost
 
 
 EIG_METHODS = {"determinant": 0, "mineigval": 1, "invtraceinv": 2}

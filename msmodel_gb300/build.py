@@ -76,7 +76,8 @@ def build(force=False, verbose=False):
                 if verbose:
                     print("built", out)
     if force or jobs or _stale(LIB, objs):
-        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"]
+        # cuSOLVER: the general eigenproblem behind msgpu_eigvals_batch (not the hot path)
+        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcusolver", "-lm"]
         _compile((cmd, LIB))
     return LIB
 

@@ -240,6 +240,7 @@ class Reference:
         L.ref_save_cdata.argtypes = [C.c_int, _dp, C.c_char_p]
         L.ref_parse_cdata.argtypes = [C.c_int, C.c_char_p, _dp]
         L.ref_traceinv.argtypes = med + [C.c_int, _dp, _dp]
+        L.ref_eigvals.argtypes = med + [_dp, _dp]
         L.ref_inverse_iteration.argtypes = med + [_dp, _dp, _dp]
         L.ref_roots_muller.argtypes = [C.c_int] + med + [_dp, C.c_int, _dp, C.c_int, C.c_double]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
@@ -289,6 +290,11 @@ class Reference:
 
     def total_cross_section(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
         return self.L.ref_total_cross_section(*self._med(d, n, model, params, shape, ratio, seed), float(k))
+
+    def eigvals(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
+        mu = np.zeros(2 * n)
+        self.L.ref_eigvals(*self._med(d, n, model, params, shape, ratio, seed), np.array([k.real, k.imag]), mu)
+        return mu.view(np.complex128).copy()
 
     def traceinv(self, d, n, seed, ks, model="maximum", params=(), shape="ball", ratio=1.0):
         kk = _cplx_array(ks)

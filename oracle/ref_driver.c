@@ -266,3 +266,15 @@ int ref_roots_muller(int method, int d, int n, int mtype, int np, const double* 
     drop_medium(&med);
     return nroot;
 }
+
+/* eigvals (ms_matrix_util.c:147, zgeev_) of M(k) */
+void ref_eigvals(int d, int n, int mtype, int np, const double* p, int shape, double ratio, unsigned long seed,
+                 const double* k, double* mu) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    dcomplex* a = (dcomplex*)malloc(sizeof(dcomplex) * (size_t)n * n);
+    build_ms_matrix(&med, k[0] + I * k[1], a);
+    eigvals(n, a, (dcomplex*)mu);
+    free(a);
+    drop_medium(&med);
+}

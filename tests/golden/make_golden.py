@@ -161,6 +161,9 @@ def reference_runs():
         roots = r.roots_muller(method, 3, 100, 1, dom, z0, maxit=30, toler=1e-10)
         add("roots_muller", method=method, d=3, n=100, seed=1, dom=dom, z0=_cl(z0), maxit=30, toler=1e-10,
             roots=_cl(roots))
+    # eigenvalues of M(k) (eigvals, zgeev): the input of the mu-plane histograms
+    for d, n, seed, k in ((3, 60, 1, 1.2 - 0.05j), (2, 50, 2, 0.8 + 0.0j)):
+        add("eigvals", d=d, n=n, seed=seed, k=[k.real, k.imag], mu=_cl(r.eigvals(d, n, seed, k)))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)

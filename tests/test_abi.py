@@ -90,3 +90,16 @@ def test_tuning_table_host_side():
     finally:
         ms.tune_set("dlogf", "mixed", 300, None, 0)
     assert ms.tune_table() == []
+
+
+def test_imag_mu_histogram_restates_reference_binning():
+    """Log-spaced bins, samples outside (or with Im mu <= 0) lost, unit integral
+    with each bin divided by its width (imag_mu_histogram_util.c:108-153)."""
+    import msmodel_gb300 as ms
+    mu = [np.array([1e-3j, 2e-2j, 0.5j, -1j, 3j, 0.9 + 0.2j])]
+    dens, centres, lost = ms.imag_mu_histogram(mu, 4, 1e-3, 1.0)
+    assert lost == 2
+    width = np.log(1e3) / 4
+    assert abs(np.sum(dens * centres * width) - 1.0) < 1e-14
+    counts = dens * centres * 4 * width
+    assert np.allclose(counts, [1, 1, 0, 2])  # bin edges 1e-3, 5.6e-3, 3.2e-2, 0.18, 1
