@@ -10,6 +10,9 @@ appends the section it names with the same keys, order and number formats:
                      (color line: save_colorrule, color_rule_util.c:276-282)
   [kcut]             save_complexcut       src/core/complex_cut_util.c:106-117
   [random_function]  save_random_function  src/core/random_function_util.c:178-193
+  [eigenstate_list]  save_eigenstate_list  src/core/eigenstate_list_util.c:296-314
+                     (domain: save_domain, domain_util.c:83; states: save_eigenstate,
+                     eigenstate_util.c:202-213)
   data= line         save_cdata            src/core/complex_data_util.c:21-28
 
 `parse_cdata` reads a data= line back (parse_complex_data,
@@ -19,7 +22,7 @@ conversions (%g, %.16g, %+.16g), which Python's % operator reproduces.
 import numpy as np
 
 __all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
-           "save_random_function"]
+           "save_random_function", "save_eigenstate_list"]
 
 MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
@@ -85,3 +88,18 @@ def save_random_function(fname, kind, data, xmin, xmax, title="", realtime=0.0):
             % (title, kind, nseed, nbin, xmin, xmax, realtime))
     text += "data=" + "".join("%.16g " % v for v in data.reshape(-1)) + "\n\n"
     _append(fname, text)
+
+
+def save_eigenstate_list(fname, states, seed, method, ntarget, dom, maxit, toler, realtime=0.0, verb=0):
+    """An [eigenstate_list] section; states = [(kroot, mu, eigenvector)] as
+    find_eigenstates(..., eigenvectors=True) returns them for one medium."""
+    text = ("[eigenstate_list]\nseed=%d\nmethod=%s\nntarget=%d\nnstate=%d\n"
+            % (seed, method, ntarget, len(states)))
+    text += "xrange=%.16g:%.16g\nyrange=%.16g:%.16g\n" % (dom[0], dom[1], dom[2], dom[3])
+    text += "maxit=%d\ntoler=%g\nverb=%d\nrealtime=%g\n" % (maxit, toler, verb, realtime)
+    for i, (k, mu, v) in enumerate(states):
+        k, mu = complex(k), complex(mu)
+        text += "st%d_kroot=%.16g%+.16gi\n" % (i, k.real, k.imag)
+        text += "st%d_mu=%.16g%+.16gi\n" % (i, mu.real, mu.imag)
+        text += "st%d_eigv=" % i + "".join("%.16g%+.16gi " % (z.real, z.imag) for z in np.asarray(v)) + "\n"
+    _append(fname, text + "\n")

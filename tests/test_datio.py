@@ -54,3 +54,15 @@ def test_sections(tmp_path):
     assert "[random_function]\ntitle=DOS\ntype=dos\nnseed=2\nnbin=2\nxmin=0.4\nxmax=3.5\nrealtime=2\n" \
            "data=1 2 3 4.5 \n\n" in text
     assert "xrange=0.5:3\nyrange=-0.5:0\ncolor=magma seq 3\ndata=0+1i 2+0i 3+0i 4+0i \n\n" in text
+
+
+def test_eigenstate_list_section(tmp_path):
+    f = str(tmp_path / "eig.dat")
+    states = [(1.5 - 0.02j, 1e-12 + 2e-13j, np.array([0.6 + 0j, 0.8j])), (2.25 - 0.5j, complex(0.0, -3e-11), np.array([1, 0]))]
+    datio.save_eigenstate_list(f, states, 7, "determinant", 32, (0.5, 3, -1, 0), 30, 1e-10)
+    text = open(f).read()
+    assert text.startswith("[eigenstate_list]\nseed=7\nmethod=determinant\nntarget=32\nnstate=2\n"
+                           "xrange=0.5:3\nyrange=-1:0\nmaxit=30\ntoler=1e-10\nverb=0\nrealtime=0\n")
+    assert "st0_kroot=1.5-0.02i\nst0_mu=1e-12+2e-13i\nst0_eigv=0.6+0i 0+0.8i \n" in text
+    assert "st1_kroot=2.25-0.5i\nst1_mu=0-3e-11i\nst1_eigv=1+0i 0+0i \n\n" in text
+    assert datio.parse_cdata("data=" + text.split("st0_eigv=")[1].split("\n")[0]).tolist() == [0.6, 0.8j]
