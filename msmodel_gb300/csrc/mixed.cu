@@ -155,19 +155,20 @@ extern "C" int msgpu_probe_umma(int mode, const float* A, const float* B, float*
     float *dA = nullptr, *dB = nullptr, *dD = nullptr;
     int* derr = nullptr;
     int herr = 0;
+    auto done = [&](int rc) {
+        cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(derr);
+        return rc;
+    };
     if (cudaMalloc(&dA, 128 * 32 * 4) || cudaMalloc(&dB, 64 * 32 * 4) || cudaMalloc(&dD, 128 * 64 * 4) ||
         cudaMalloc(&derr, 4))
-        return MSGPU_E_CUDA;
-    cudaMemcpy(dA, A, 128 * 32 * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(dB, B, 64 * 32 * 4, cudaMemcpyHostToDevice);
-    cudaMemset(dD, 0, 128 * 64 * 4);
-    cudaMemset(derr, 0, 4);
-    cudaFuncSetAttribute(k_probe_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536);
+        return done(MSGPU_E_CUDA);
+    if (cudaMemcpy(dA, A, 128 * 32 * 4, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(dB, B, 64 * 32 * 4, cudaMemcpyHostToDevice) || cudaMemset(dD, 0, 128 * 64 * 4) ||
+        cudaMemset(derr, 0, 4) || cudaFuncSetAttribute(k_probe_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536))
+        return done(MSGPU_E_CUDA);
     k_probe_umma<<<1, 128, 65536>>>(dA, dB, dD, mode, derr);
-    cudaError_t e = cudaDeviceSynchronize();
-    cudaMemcpy(D, dD, 128 * 64 * 4, cudaMemcpyDeviceToHost);
-    cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost);
-    cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(derr);
-    if (e != cudaSuccess) return MSGPU_E_CUDA;
-    return herr ? MSGPU_E_CUDA : 0;
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(D, dD, 128 * 64 * 4, cudaMemcpyDeviceToHost) || cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost))
+        return done(MSGPU_E_CUDA);
+    return done(herr ? MSGPU_E_CUDA : 0);
 }

@@ -181,9 +181,11 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
         cleanup();
         return MSGPU_E_CUDA;
     }
-    cudaMemset(dfun, 0, sizeof(double) * plane);
-    cudaMemset(dden, 0, sizeof(double) * plane);
-    cudaMemcpy(dks, ks, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice);
+    if (cudaMemset(dfun, 0, sizeof(double) * plane) || cudaMemset(dden, 0, sizeof(double) * plane) ||
+        cudaMemcpy(dks, ks, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice)) {
+        cleanup();
+        return MSGPU_E_CUDA;
+    }
     GridArgs A;
     A.d = d;
     A.n = n;
@@ -200,9 +202,12 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
     A.den = dden;
     const dim3 grid((unsigned)((np + PT - 1) / PT), (unsigned)nk);
     for (int m = 0; m < nmed; ++m) {
-        cudaMemcpy(dpos, media[m].pos, sizeof(double) * (size_t)n * d, cudaMemcpyHostToDevice);
-        cudaMemcpy(damp, a.data() + 2 * (size_t)m * nk * n, sizeof(double) * 2 * (size_t)nk * n,
-                   cudaMemcpyHostToDevice);
+        if (cudaMemcpy(dpos, media[m].pos, sizeof(double) * (size_t)n * d, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(damp, a.data() + 2 * (size_t)m * nk * n, sizeof(double) * 2 * (size_t)nk * n,
+                       cudaMemcpyHostToDevice)) {
+            cleanup();
+            return MSGPU_E_CUDA;
+        }
         A.psi = m == 0 ? dpsi : nullptr;
         if (use_df) k_psi_grid_df3<<<grid, PT>>>(A);
         else k_psi_grid<<<grid, PT>>>(A);
