@@ -59,6 +59,24 @@ def dist_env():
     return ws, rank, lr
 
 
+TRAFFIC_FILE = os.path.join("profiles", "dram_traffic.json")
+
+
+def recorded_traffic(precision, points):
+    """DRAM bytes of one engine launch over `points` cut points at N=1024: the
+    per-ln-det bytes of an ncu capture (dram__bytes_read + write of one
+    304-point launch, recorded in the data file TRAFFIC_FILE with its command)
+    times the points.  Not measured by this run: ncu cannot run inside it."""
+    try:
+        with open(os.path.join(ROOT, TRAFFIC_FILE)) as f:
+            rec = json.load(f)["kcut_d3_n1024"][precision]
+    except (OSError, KeyError, ValueError):
+        return None, "no recorded capture"
+    per_eval = (rec["dram_read"] + rec["dram_write"]) / rec["points"]
+    return per_eval * points, (f"recorded ncu capture ({TRAFFIC_FILE}: {rec['kernel']}, one {rec['points']}-point "
+                               f"launch), per-ln-det bytes x {points} points")
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -115,29 +133,48 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(seconds=15.0, nk_cap=NK):
+def oracle_cut(o):
+    """The 4096 cut points and the N=1024 seed-1 positions from the oracle
+    alone (the reference arm and the CPU baselines load no library of this
+    package): central samples of the reference kcut, get_arg_ccut order."""
+    ks = o.kcut_args(NK, KMIN, KMAX)[4::3][:NK].copy()
+    return ks, o.fill_medium(D, N, 1)
+
+
+def strided_sample(ks, step, per_step, stride=128):
+    """`per_step` cut points for step `step`, strided across the whole cut:
+    offsets step, step + stride, ... (mod stride), so that successive steps
+    walk every residue class and the sample spans Re k in [0.5, 3]."""
+    out = []
+    r = step
+    while len(out) < per_step:
+        out.extend(ks[r % stride::stride][: per_step - len(out)])
+        r += 1
+    return np.asarray(out)
+
+
+def cpu_baseline(seconds=15.0):
     """The reference algorithm (oracle port: reference assembly + OpenBLAS
     zgetrf, one LAPACK thread per OpenMP thread, as run_tracelog_omp) on all
-    host cores, on a bounded sample of the same cut."""
+    host cores, on a bounded sample of the same cut strided across all 4096 k."""
     from oracle import Oracle
-    from msmodel_gb300 import fill_medium
     o = Oracle()
     threads = os.cpu_count() or 1
-    pos = fill_medium(D, N, 1)
-    ks = workload_ks()
+    ks, pos = oracle_cut(o)
+    per_chunk = 2 * threads
     done, t0, i = 0, time.perf_counter(), 0
     while True:
-        chunk = ks[(i * threads) % nk_cap:(i * threads) % nk_cap + threads]
+        chunk = strided_sample(ks, i, per_chunk)
         o.tracelog_batch(D, N, pos, chunk, nthreads=threads)
         done += len(chunk)
         i += 1
         el = time.perf_counter() - t0
         if el >= seconds and i >= 2:
             break
-    # the oracle port: the reference's compiled sources are not on the GPU host
     return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {done} of the 4096 cut points, N=1024 d=3 seed 1, {threads} OpenMP threads x "
-                      f"1 OpenBLAS thread ({o.lapack_config().split()[0:2]})", "seconds": el}
+            "sample": f"{done} of the 4096 cut points taken every 128th across the cut (offsets 0..{i - 1}), "
+                      f"N=1024 d=3 seed 1, {threads} OpenMP threads x 1 OpenBLAS thread "
+                      f"({' '.join(o.lapack_config().split()[0:2])})", "seconds": el}
 
 
 def measure_mixed(ms, torch, med, ks, out64, args, stream, flush, ws, barrier):
@@ -187,13 +224,10 @@ def measure_mixed(ms, torch, med, ks, out64, args, stream, flush, ws, barrier):
                                       "points": int(relerr.size)},
             "im_branch_max_dist": float(np.max(np.abs(((lndm.imag - lnd64.imag) + np.pi) % (2 * np.pi) - np.pi))),
             "roofline": {"bound": "tensor", "achieved": tensor_flops / 1e12,
-                         "traffic": ((115677166336 + 99175409408) / 304 * len(ks)) if n == N else None,
+                         "traffic": recorded_traffic("mixed", len(ks))[0] if n == N else None,
                          "peak": read_peaks().get("bf16_tflops_sustained", 1728.6), "unit": "TFLOP/s",
                          "frac": tensor_flops / 1e12 / read_peaks().get("bf16_tflops_sustained", 1728.6),
                          "counted": "bf16 tensor flops executed (80/3 n^3 per ln det)",
-                         "observed": "not tensor-bound: ncu at N=512 (profiles/k_engine_mixed_kcut_n512.md) shows "
-                                     "FP32 pipe 26%, tensor 3.7%, FP64 4%, DRAM 29% of peak, stalls on global "
-                                     "memory and barriers (double-float panel, TRSM, trailing-matrix round trips)",
                          "algorithmic_tflops": 8.0 / 3.0 * n ** 3 * len(ks) / (tot / args.steps) / 1e12}}
 
 
@@ -257,6 +291,12 @@ def measure_aberth(ms, torch, count, cpu_sample):
         nr = sum(len(r) for r in outs)
         res["cpu_baseline"] = {"roots_per_s": nr / el, "roots": nr, "realisations": len(sample),
                                "cores": os.cpu_count(), "kind": "port", "seconds": el}
+        # the GPU searches against the oracle's root lists on the same realisations
+        for prec in ("fp64", "mixed"):
+            got = roots[prec][:len(sample)]
+            res[prec + "_matches_oracle"] = {
+                "matched": sum(match_count(got[i], outs[i], 1e-8) for i in range(len(sample))),
+                "oracle_roots": nr, "gpu_roots": sum(len(r) for r in got), "realisations": len(sample)}
     res["config"] = {"realisations": count, "natom": "100..600 (reference generator, seed 0)", "seeds": 32,
                      "domain": ABERTH_DOM, "nexpsup": 4, "maxit": 30, "toler": 1e-10}
     return res
@@ -464,35 +504,39 @@ def run_workload(args):
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores: the oracle port (reference
+    assembly restated + LAPACK zgetrf, OpenMP over points with one LAPACK
+    thread each, as run_tracelog_omp).  Positions and k come from the oracle;
+    nothing of this package is loaded.  Each step is a bounded sample of the
+    cut: 2 points per host thread, strided across all 4096 k."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     from oracle import Oracle
-    from msmodel_gb300 import fill_medium
     o = Oracle()
     threads = os.cpu_count() or 1
-    pos = fill_medium(D, N, 1)
-    ks = workload_ks()
+    ks, pos = oracle_cut(o)
     per_step = threads * 2
     for w in range(args.warmup):
-        o.tracelog_batch(D, N, pos, ks[:threads], nthreads=threads)
+        o.tracelog_batch(D, N, pos, strided_sample(ks, 127 - w, threads), nthreads=threads)
     t0 = time.perf_counter()
     done = 0
     for s in range(args.steps):
-        off = (s * per_step) % NK
-        o.tracelog_batch(D, N, pos, ks[off:off + per_step], nthreads=threads)
+        o.tracelog_batch(D, N, pos, strided_sample(ks, s, per_step), nthreads=threads)
         done += per_step
     el = time.perf_counter() - t0
     v = done / el
+    sample = (f"{per_step} cut points per step taken every 128th across the 4096-point cut (step s: offsets "
+              f"s, s+1, ...), {threads} OpenMP threads x 1 OpenBLAS thread, reference assembly restated + "
+              "LAPACK zgetrf")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
             "data": "synthetic (seeded scatterers, reference generator)",
             "config": {"workload": "kcut d=3 N=1024 4096k Im=-0.05", "d": D, "natom": N, "nk": NK,
-                       "model": "maximum", "shape": "ball", "sample_per_step": per_step},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{per_step} cut points per step, {threads} OpenMP threads x 1 OpenBLAS "
-                                       "thread, reference assembly restated + LAPACK zgetrf"},
+                       "model": "maximum", "shape": "ball", "sample_per_step": per_step,
+                       "sample": "strided across the whole cut (every 128th point)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -590,12 +634,8 @@ def main():
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained",
                 "algorithmic": "8/3 N^3 real flops per ln det", "traffic": None}
-    # DRAM bytes per ln det at N=1024 from one ncu capture of a full wave
-    # (profiles/engine_dram_traffic_kcut_n1024.md), scaled to this launch's points
     if natom == N:
-        per_eval = {"fp64": (108366984448 + 79019248640) / 304, "mixed": (115677166336 + 99175409408) / 304}
-        roof["traffic"] = per_eval[args.precision] * len(ks)
-        roof["traffic_source"] = "ncu dram__bytes_read+write of a 304-point wave, x points/304"
+        roof["traffic"], roof["traffic_source"] = recorded_traffic(args.precision, len(ks))
 
     e2e = None
     if not args.no_e2e:

@@ -142,9 +142,15 @@ int msgpu_amplitude_batch(int nmed, const msgpu_medium* media, int nitem, const 
  * the work is queued on `stream` (cudaStream_t or NULL) and the call returns
  * without synchronizing.  Scratch is a fixed 128 MiB __device__ array inside
  * the library (held by every GPU that loads it): n <= 2048, nk <= 65536, else
- * MSGPU_E_SIZE.  Calls share that array, so calls that overlap on the GPU
- * race: keep them on one stream.  The first call on a device looks up the
- * array's address; make it before any stream capture. */
+ * MSGPU_E_SIZE.  The array holds floor(~128 MiB / (16 n^2)) matrix slots, one
+ * per engine CTA, capped at 2 per SM: 304 CTAs for n <= 165, 127 at n = 256,
+ * 31 at n = 512, 7 at n = 1024 and 1 at n = 2048, against the 304 the
+ * allocating entry points run, so large n runs at a fraction of their
+ * throughput (1/43 at n = 1024).  Calls share that array, so calls that
+ * overlap on the GPU race: keep them on one stream.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * Counted in msgpu_launch_count (two launches per call); errors set the text
+ * of msgpu_last_error. */
 int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, msgpu_model model, int nk, const double* d_ks,
                                  double* d_out, int* d_status, void* stream);
 
@@ -177,7 +183,11 @@ int msgpu_wave_function(int nmed, const msgpu_medium* media, const double* k, in
  * media[0]) are k-major, amps[nmed][nk][n].  MSGPU_MIXED solves with the
  * mixed engine plus FP64-residual refinement and, for d = 3, evaluates the
  * Green functions of the grid in double-float arithmetic on the FP32 pipe
- * (|Im k| * r < 80 over the grid; otherwise FP64). */
+ * (|Im k| * r < 80 over the grid; otherwise FP64).  Both return a negative
+ * MSGPU_E_* code on error, else the OR of the MSGPU_S_* status words of every
+ * solve: 0 when all are clean, MSGPU_S_SINGULAR or MSGPU_S_NONFINITE when a
+ * singular or non-finite solve was averaged into function and density (the
+ * reference's zgesv_ loop, ms_core.c:620, goes on silently in that case). */
 int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, int nk, const double* ks, int nx, int ny,
                               const double* dom, double* function, double* density, double* psi, double* amps,
                               int precision);

@@ -8,6 +8,7 @@ goes through the C ABI declared in include/msgpu.h; there is no CPU path:
 if the CUDA library is missing or no GPU is present the calls raise.
 """
 import ctypes as C
+import warnings
 import os
 
 import numpy as np
@@ -410,10 +411,15 @@ def wave_function_batch(media, ks, nx, ny, dom, precision="fp64", want_psi=True)
     psi = np.zeros(2 * nk * npx) if want_psi else None
     amps = np.zeros(2 * len(media) * nk * n)
     arr = _media_array(media)
-    _check(lib().msgpu_wave_function_batch(len(media), arr, nk, ks.view(np.float64), nx, ny,
-                                           np.asarray(dom, dtype=np.float64), fun, den,
-                                           psi.ctypes.data if want_psi else None, amps.ctypes.data,
-                                           PRECISION[precision]), "wave_function_batch")
+    rc = lib().msgpu_wave_function_batch(len(media), arr, nk, ks.view(np.float64), nx, ny,
+                                         np.asarray(dom, dtype=np.float64), fun, den,
+                                         psi.ctypes.data if want_psi else None, amps.ctypes.data,
+                                         PRECISION[precision])
+    if rc < 0:
+        _check(rc, "wave_function_batch")
+    if rc > 0:
+        warnings.warn(f"wave_function_batch: a solve returned status {rc:#x} "
+                      f"(singular or non-finite amplitudes were averaged in)", RuntimeWarning, stacklevel=2)
     a = amps.view(np.complex128).reshape(len(media), nk, n)
     return (fun.reshape(nk, npx), den.reshape(nk, npx),
             psi.view(np.complex128).reshape(nk, npx) if want_psi else None, [a[m].copy() for m in range(len(media))])

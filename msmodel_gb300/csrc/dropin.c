@@ -123,8 +123,16 @@ void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread
             im[it] = s;
         }
     }
-    int e = msgpu_tracelog_batch(nseed, media, nseed * ntot, im, ks, out, NULL, MSGPU_FP64);
+    int* st = (int*)calloc((size_t)nseed * ntot, sizeof(int));
+    int e = msgpu_tracelog_batch(nseed, media, nseed * ntot, im, ks, out, st, MSGPU_FP64);
     if (e) fail("run_tracelog_omp", e);
+    /* the reference's tracelog_lu warns once per singular matrix (ms_matrix_util.c:188-190); the
+     * pivot index is not kept per item, so the warning names the matrix's point and seed instead */
+    for (size_t it = 0; it < (size_t)nseed * ntot; it++)
+        if (st[it] & MSGPU_S_SINGULAR)
+            printf("[LAPACK] Element U(i,i) is exactly zero, the determinant will be singular (seed %d, point %d).\n",
+                   (int)(it / ntot) + 1, (int)(it % ntot));
+    free(st);
     /* running average over seeds in seed order (ms_core.c:127) */
     for (int s = 1; s <= nseed; s++)
         for (int l = 0; l < ntot; l++) {

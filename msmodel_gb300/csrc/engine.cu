@@ -322,6 +322,7 @@ extern "C" {
 
 namespace msg {
 void count_launches(int n) { g_launches += n; }
+int record_error(int code, const char* what) { return set_err(code, what); }
 }  // namespace msg
 
 extern "C" {

@@ -34,6 +34,8 @@ struct EngineParams {
 
 // adds to the library's count of kernel launches (msgpu_launch_count)
 void count_launches(int n);
+// sets the text msgpu_last_error returns and passes `code` through
+int record_error(int code, const char* what);
 
 // Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
 // negative MSGPU_E* code on error.

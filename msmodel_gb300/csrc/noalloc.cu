@@ -60,22 +60,27 @@ int g_na_sms[64] = {0};
 extern "C" int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, msgpu_model model, int nk,
                                             const double* d_ks, double* d_out, int* d_status, void* stream) {
     using namespace msg;
-    if (d < 1 || d > 20 || n < 1 || nk < 1 || !d_pos || !d_ks || !d_out || !d_status) return MSGPU_E_ARG;
-    if (n > NOALLOC_MAX_N || nk > NOALLOC_MAX_ITEMS) return MSGPU_E_SIZE;
+    if (d < 1 || d > 20 || n < 1 || nk < 1 || !d_pos || !d_ks || !d_out || !d_status)
+        return record_error(MSGPU_E_ARG, "noalloc: bad argument (d in 1..20, n >= 1, nk >= 1, non-null pointers)");
+    if (n > NOALLOC_MAX_N || nk > NOALLOC_MAX_ITEMS)
+        return record_error(MSGPU_E_SIZE, "noalloc: n > 2048 or nk > 65536 exceeds the fixed scratch array");
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MSGPU_E_NODEV;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return record_error(MSGPU_E_NODEV, "noalloc: cudaGetDevice failed or device index beyond 63");
     void* base = nullptr;
     int sms = 0;
     {
         std::lock_guard<std::mutex> lk(g_na_mu);
         if (!g_na_addr[dev]) {
             void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return MSGPU_E_CUDA;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+                return record_error(MSGPU_E_CUDA, "noalloc: cudaGetSymbolAddress of the scratch array failed");
             if (cudaFuncSetAttribute(k_engine_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sizeof(LuSmem)) != cudaSuccess)
-                return MSGPU_E_CUDA;
+                return record_error(MSGPU_E_CUDA, "noalloc: cudaFuncSetAttribute(k_engine_fp64) failed");
             int nsm = 0;
-            if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MSGPU_E_CUDA;
+            if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+                return record_error(MSGPU_E_CUDA, "noalloc: cudaDeviceGetAttribute(SM count) failed");
             g_na_sms[dev] = nsm;
             g_na_addr[dev] = p;
         }
@@ -92,13 +97,14 @@ extern "C" int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, m
     size_t grid = (NOALLOC_BYTES - NOALLOC_HEADER - 256) / per_cta;
     if (grid > (size_t)(2 * sms)) grid = 2 * sms;
     if (grid > (size_t)nk) grid = nk;
-    if (grid < 1) return MSGPU_E_SIZE;
+    if (grid < 1) return record_error(MSGPU_E_SIZE, "noalloc: one matrix slot does not fit the scratch array");
     const size_t ws_off = (NOALLOC_HEADER + 255) / 256 * 256;
     zc* ws = reinterpret_cast<zc*>(b + ws_off);
     int* piv = reinterpret_cast<int*>(b + ws_off + grid * slot * sizeof(zc));
     cudaStream_t st = (cudaStream_t)stream;
     MedDev v{d, n, d_pos, model};
     k_noalloc_setup<<<(nk + 255) / 256, 256, 0, st>>>(md, v, counter, item_med, order, nk);
+    if (cudaGetLastError() != cudaSuccess) return record_error(MSGPU_E_CUDA, "noalloc: set-up kernel launch failed");
     EngineParams P;
     P.media = md;
     P.ks = d_ks;
@@ -116,5 +122,7 @@ extern "C" int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, m
     P.amps = nullptr;
     P.amp_off = nullptr;
     k_engine_fp64<<<(unsigned)grid, NT, sizeof(LuSmem), st>>>(P);
-    return cudaGetLastError() == cudaSuccess ? 0 : MSGPU_E_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return record_error(MSGPU_E_CUDA, "noalloc: engine kernel launch failed");
+    count_launches(2);
+    return 0;
 }

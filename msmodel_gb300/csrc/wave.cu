@@ -227,7 +227,10 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
         function[l] /= nmed;
         density[l] /= nmed;
     }
-    return 0;
+    // the solves' status words, OR-ed: a singular or non-finite solve reached the averages
+    int any = 0;
+    for (int v : st) any |= v;
+    return any;
 }
 
 // Seed-averaged wavefunction of run_wave_function_omp at one wave number k.

@@ -2,7 +2,9 @@
 
 * ``oracle/liboracle.so`` -- the C restatement in ``msoracle.c`` (always).
 * ``oracle/_ref/libmsref.so`` -- the reference MSModel sources compiled
-  unmodified from ``/root/reference/src/core`` together with
+  unmodified from ``$MSMODEL_REF/src/core`` (the reference tree, given by the
+  environment variable MSMODEL_REF or ``--ref``; default ``/root/reference``)
+  together with
   ``ref_driver.c`` and ``lapack_shim.c``; only where the reference tree
   exists (it is absent on GPU machines, where the oracle alone is used).
 
@@ -14,7 +16,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("MSMODEL_REF", "/root/reference")
 # the reference's hot-path translation units (and what they pull in)
 REF_SOURCES = [
     "ms_matrix_util.c", "green_bessel.c", "medium_util.c", "nru_random.c",
@@ -54,8 +56,8 @@ def build_oracle(force=False):
     return out
 
 
-def build_ref(force=False):
-    core = os.path.join(REF_ROOT, "src", "core")
+def build_ref(force=False, ref_root=None):
+    core = os.path.join(ref_root or REF_ROOT, "src", "core")
     if not os.path.isdir(core):
         return None
     ob = openblas_path()
@@ -74,5 +76,9 @@ def build_ref(force=False):
 
 
 if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=None, help="reference tree (default: $MSMODEL_REF or /root/reference)")
+    a = ap.parse_args()
     print(build_oracle(force=True))
-    print(build_ref(force=True))
+    print(build_ref(force=True, ref_root=a.ref))

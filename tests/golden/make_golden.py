@@ -14,7 +14,7 @@ time reads the reference).
    its sources into oracle/_ref, on the hot-path configurations at sizes that
    finish in seconds (seeded scatterers, ln det / N, dlogf, roots, psi).
 
-Usage:  python tests/golden/make_golden.py
+Usage:  [MSMODEL_REF=<reference tree>] python tests/golden/make_golden.py
 """
 import ast
 import hashlib
@@ -27,7 +27,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+# the reference tree: $MSMODEL_REF, default /root/reference
+REF = os.environ.get("MSMODEL_REF", "/root/reference")
 sys.path.insert(0, ROOT)
 
 

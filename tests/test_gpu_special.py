@@ -14,15 +14,18 @@ def _rows(ref_tests, name):
 
 @pytest.mark.parametrize("name,which", [("GREEN_DATA", 0), ("DK_GREEN_DATA", 1), ("GREEN_IMAG_DATA", 2)])
 def test_green_tables(ms, ref_tests, name, which):
+    # every dimension of the tables (d in -2..5, 10, 20), each bounded on its own
     rows = _rows(ref_tests, name)
-    errs = []
+    errs, worst = [], {}
     for d in np.unique(rows[:, 0]).astype(int):
         sel = rows[rows[:, 0] == d]
         got = ms.eval_special(which, int(d), sel[:, 1] + 1j * sel[:, 2], 1.0)
-        errs.append(rel(got, sel[:, 3] + 1j * sel[:, 4]) if abs(d) <= 5 else np.minimum(rel(got, sel[:, 3] + 1j * sel[:, 4]), 1e-12))
+        e = rel(got, sel[:, 3] + 1j * sel[:, 4])
+        worst[int(d)] = float(np.max(e))
+        errs.append(e)
     e = np.concatenate(errs)
     assert np.median(e) < 1e-14
-    assert np.max(e) < 1e-11
+    assert max(worst.values()) < 1e-11, worst
 
 
 def test_bessel_k_table(ms, ref_tests):

@@ -72,3 +72,19 @@ def test_double_float_grid(ms, k):
     want, scale = _psi_fp64(med.pos, amps[0], k, 23, 19, dom)
     err = np.max(np.abs(psi - want) / scale)
     assert err < 1e-12, err
+
+
+def test_wave_singular_solve_is_reported(ms):
+    """Two scatterers at the same point make M(k) non-finite (G(k, 0) diverges):
+    the batch returns that solve's status bits instead of averaging it in silently."""
+    med = ms.Medium(3, 40, seed=1)
+    pos = med.pos.copy()
+    pos[3:6] = pos[0:3]
+    bad = ms.Medium(3, 40, pos=pos, seed=1)
+    dom = [-2.0, 2.0, -2.0, 2.0]
+    with pytest.warns(RuntimeWarning, match="status"):
+        ms.wave_function_batch([bad], [1.5 + 0j], 8, 8, dom, want_psi=False)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        ms.wave_function_batch([med], [1.5 + 0j], 8, 8, dom, want_psi=False)

@@ -16,19 +16,16 @@ def test_green_goldens(oracle, ref_tests):
     rows = _rows(ref_tests, "GREEN_DATA")
     errs = np.array([abs(oracle.free_green(int(r[0]), complex(r[1], r[2]), 1.0) / complex(r[3], r[4]) - 1)
                      for r in rows])
-    small = np.abs(rows[:, 0]) <= 5
     assert np.median(errs) < 1e-14
-    assert np.max(errs[small]) < 1e-11
-    assert np.mean(errs) < 1e-11
+    assert np.max(errs) < 1e-11
 
 
 def test_dk_green_goldens(oracle, ref_tests):
     rows = _rows(ref_tests, "DK_GREEN_DATA")
     errs = np.array([abs(oracle.dk_free_green(int(r[0]), complex(r[1], r[2]), 1.0) / complex(r[3], r[4]) - 1)
                      for r in rows])
-    small = np.abs(rows[:, 0]) <= 5
     assert np.median(errs) < 1e-14
-    assert np.max(errs[small]) < 1e-11
+    assert np.max(errs) < 1e-11
 
 
 def test_bessel_k_goldens(oracle, ref_tests):
