@@ -50,6 +50,36 @@ def run_tracelog_sharded(d, n, ks, nseed, rank, world, compute=None, gather=None
     return seed_average([allv[s] for s in range(1, nseed + 1)])
 
 
+def split_points(npoint, rank, world):
+    """Point indices of this rank when the points of one realisation are split
+    over `world` ranks: contiguous blocks, the first npoint % world ranks one
+    point longer (strong scaling of a complex cut or map)."""
+    base, extra = divmod(npoint, world)
+    start = rank * base + min(rank, extra)
+    return np.arange(start, start + base + (1 if rank < extra else 0))
+
+
+def run_cut_sharded(ks, rank, world, compute, gather=None):
+    """ln det/n of one realisation at every k of a cut or map, the points split
+    over `world` ranks (split_points); each rank evaluates its block on its GPU
+    with no data-path collective, and one gather returns every rank the whole
+    result in point order.
+
+    compute(ks block) -> complex array over the block.
+    gather(obj) -> list of every rank's obj (e.g. torch.distributed.all_gather_object)."""
+    ks = np.atleast_1d(np.asarray(ks, dtype=np.complex128))
+    idx = split_points(len(ks), rank, world)
+    mine = (int(idx[0]) if len(idx) else 0, np.asarray(compute(ks[idx]) if len(idx) else np.zeros(0, complex)))
+    parts = gather(mine) if gather is not None else [mine]
+    out = np.empty(len(ks), dtype=np.complex128)
+    seen = 0
+    for start, vals in sorted(parts, key=lambda p: p[0]):
+        out[start:start + len(vals)] = vals
+        seen += len(vals)
+    assert seen == len(ks), "missing points after gather"
+    return out
+
+
 def deal_by_cost(costs, world):
     """Indices dealt to `world` ranks, largest cost first, each to the rank with
     the least work so far (ties to the lowest rank): the uneven realisation

@@ -118,3 +118,50 @@ def test_two_rank_resonance_search_gathers_roots_and_histogram():
         for r in roots:
             assert np.array_equal(roots[r], want[r])
         assert np.array_equal(hist, want_hist) and hist.sum() == allr.size
+
+
+def _cut_worker(rank, world, port, q):
+    import torch.distributed as dist
+    from msmodel_gb300.sharding import run_cut_sharded
+    from oracle import Oracle
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    o = Oracle()
+    pos = o.fill_medium(3, 48, 1)
+    ks = 0.5 + 2.5 * np.arange(11) / 10 - 0.05j
+
+    def compute(block):
+        return o.tracelog_batch(3, 48, pos, block, nthreads=1)[0]
+
+    def gather(obj):
+        out = [None] * world
+        dist.all_gather_object(out, obj)
+        return out
+
+    q.put((rank, run_cut_sharded(ks, rank, world, compute, gather)))
+    dist.destroy_process_group()
+
+
+def test_two_rank_cut_split_matches_single_process():
+    """Strong scaling of one realisation's cut: 11 points split in blocks of 6
+    and 5 over two ranks, one gather, the single-process cut bit for bit."""
+    import multiprocessing as mp
+    from msmodel_gb300.sharding import split_points
+    from oracle import Oracle
+    assert list(split_points(11, 0, 2)) == list(range(6)) and list(split_points(11, 1, 2)) == list(range(6, 11))
+    assert sum(len(split_points(4096, r, 8)) for r in range(8)) == 4096
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_cut_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=180) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    o = Oracle()
+    ks = 0.5 + 2.5 * np.arange(11) / 10 - 0.05j
+    want = o.tracelog_batch(3, 48, o.fill_medium(3, 48, 1), ks, nthreads=1)[0]
+    assert np.array_equal(got[0], want) and np.array_equal(got[1], want)
