@@ -16,13 +16,20 @@ sample = 4096).  One step = the hot path over the whole cut.
   clocks: nvidia-smi samples during the timed region
   gpu_launches: this library's kernel launches in the timed region
   mixed / aberth: the mixed-precision engine on the same cut, and the
-           resonance search (FP64 and mixed) over 32 realisations
+           resonance search (mixed over 256 realisations, FP64 over the first
+           32, the reference algorithm on the first 16, root lists compared)
+  configs: compact legs of the other configurations -- C1 (d=3 N=64 map),
+           C3 (d=2 N=2048 map, its 16x16 subgrid) and C5 (wavefunction
+           N=4096, 256 k; FP64 on every 16th k) -- each with both engines,
+           its accuracy against FP64 and the oracle, and a CPU baseline
 
 Other configurations print one line each with --workload map64 | map2d |
 aberth | wave.
 
-Multi-GPU (torchrun): weak scaling -- each rank evaluates the full cut for its
-own realisation (seed = rank + 1); no collective on the data path.
+Multi-GPU (torchrun): weak scaling by default -- each rank evaluates the full
+cut for its own realisation (seed = rank + 1); --scaling strong splits the
+4096 points of one realisation's cut over the ranks in contiguous blocks.  No
+collective on the data path either way.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
   python bench.py --impl reference ...   (the reference algorithm on the host cores)
@@ -257,33 +264,39 @@ def aberth_media(ms, count):
     return [ms.Medium(D, n, seed=r + 1) for r, n in enumerate(sizes)]
 
 
-def measure_aberth(ms, torch, count, cpu_sample):
+def measure_aberth(ms, torch, count, fp64_count, cpu_sample):
     """Resonance search (Aberth-Ehrlich on dlogf, 32 Halton seeds, nexpsup 4,
-    maxit 30, toler 1e-10) over `count` realisations: roots/s in FP64 and in
-    mixed precision (FP64 Newton/Aberth update), the agreement of the two root
-    sets, and the reference algorithm on `cpu_sample` realisations on all host
-    cores."""
+    maxit 30, toler 1e-10): roots/s of the mixed search (mixed dlogf far from
+    the roots, FP64 near them, FP64 update) over `count` realisations and of
+    the FP64 search over the first `fp64_count`, the agreement of their root
+    lists there, the reference algorithm on the first `cpu_sample` on all host
+    cores with both GPU searches checked against its root lists, and the
+    40-bin histogram of Im k over every mixed root."""
     media = aberth_media(ms, count)
     z0 = ms.halton_points(ABERTH_DOM, 32)
     res, roots = {}, {}
-    for prec in ("fp64", "mixed"):
+    nf = min(count, fp64_count)
+    for prec, meds in (("fp64", media[:nf]), ("mixed", media)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rs, ne = ms.solve_aberth_batch(media, ABERTH_DOM, z0, 4, 30, 1e-10, precision=prec)
+        rs, ne = ms.solve_aberth_batch(meds, ABERTH_DOM, z0, 4, 30, 1e-10, precision=prec)
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         nr = sum(len(r) for r in rs)
         roots[prec] = rs
-        res[prec] = {"roots_per_s": nr / el, "roots": nr, "dlogf_evals": ne, "dlogf_per_s": ne / el,
-                     "seconds": el}
-    found = sum(match_count(roots["mixed"][i], roots["fp64"][i], 1e-8) for i in range(count))
+        res[prec] = {"roots_per_s": nr / el, "roots": nr, "realisations": len(meds), "dlogf_evals": ne,
+                     "dlogf_per_s": ne / el, "seconds": el}
+    found = sum(match_count(roots["mixed"][i], roots["fp64"][i], 1e-8) for i in range(nf))
     res["mixed_matches_fp64"] = {"matched": found, "fp64_roots": res["fp64"]["roots"],
-                                 "mixed_roots": res["mixed"]["roots"]}
+                                 "mixed_roots": sum(len(r) for r in roots["mixed"][:nf]), "realisations": nf}
+    allim = np.concatenate([r.imag for r in roots["mixed"]]) if res["mixed"]["roots"] else np.zeros(0)
+    hist, _ = np.histogram(allim, bins=40, range=(-1.0, 0.0))
+    res["imag_histogram"] = {"range": [-1.0, 0.0], "bins": 40, "counts": hist.tolist()}
     if cpu_sample:
         import concurrent.futures as cf
         from oracle import Oracle
         o = Oracle()
-        sample = media[:cpu_sample]
+        sample = media[:min(cpu_sample, nf)]
         t0 = time.perf_counter()
         with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
             outs = list(ex.map(lambda m: o.solve_aberth(D, m.n, m.pos, ABERTH_DOM, z0)[0], sample))
@@ -485,6 +498,100 @@ def workload_wave(ms, torch, args):
     return line
 
 
+def config_legs(ms, torch, no_cpu):
+    """Compact measurements of the other configurations, carried by the
+    default line: C1 (the whole 64x64 map, both engines), C3 (the 16x16
+    subgrid of the 256x256 map, both engines) and C5 (mixed on all 256 k, FP64
+    on every 16th k).  Each reports throughput, its accuracy against FP64 and
+    the oracle, and its CPU baseline on a bounded sample."""
+    from oracle import Oracle
+    o = None if no_cpu else Oracle()
+    th = os.cpu_count() or 1
+    legs = {}
+    # C1: d=3 N=64 seed 1, 64x64 kplane on [0.5,3] x [-0.5,0]
+    med = ms.Medium(3, 64, seed=1)
+    ks = ms.kplane_args(64, 64, 0.5, 3.0, -0.5, 0.0)
+    v64, o64, s64 = _resident(ms, torch, "tracelog", [med], ks, "fp64", 3, 3)
+    vmx, omx, smx = _resident(ms, torch, "tracelog", [med], ks, "mixed", 3, 3)
+    err = np.abs((omx - o64).real) / np.abs(o64.real)
+    c1 = {"workload": "kplane d=3 N=64 64x64 Re[0.5,3] Im[-0.5,0]", "unit": "evals/s", "fp64": v64,
+          "mixed": vmx, "mixed_lndet_rel_err_vs_fp64": {"max": float(err.max()), "median": float(np.median(err))},
+          "status_nonzero": int(np.count_nonzero(s64) + np.count_nonzero(smx))}
+    if o is not None:
+        t0 = time.perf_counter()
+        ref, _ = o.tracelog_batch(3, 64, med.pos, ks, nthreads=th)
+        el = time.perf_counter() - t0
+        c1["cpu_baseline"] = {"value": len(ks) / el, "unit": "evals/s", "cores": th, "kind": "port",
+                              "sample": "the whole 4096-point map"}
+        c1["lndet_rel_err_vs_oracle"] = {
+            "fp64": float(np.max(np.abs((o64 - ref).real) / np.abs(ref.real))),
+            "mixed": float(np.max(np.abs((omx - ref).real) / np.abs(ref.real)))}
+    legs["C1"] = c1
+    # C3: d=2 N=2048 seed 1, the 16x16 subgrid (every 16th row and column) of the 256x256 map
+    med = ms.Medium(2, 2048, seed=1)
+    ks = ms.kplane_args(256, 256, 0.5, 4.0, -0.3, 0.0).reshape(256, 256)[::16, ::16].reshape(-1).copy()
+    vmx, omx, smx = _resident(ms, torch, "tracelog", [med], ks, "mixed", 1, 1)
+    v64, o64, s64 = _resident(ms, torch, "tracelog", [med], ks, "fp64", 1, 1)
+    err = np.abs((omx - o64).real * 2048) / np.abs(o64.real * 2048)
+    c3 = {"workload": "kplane d=2 N=2048 256x256 Re[0.5,4] Im[-0.3,0]: its 16x16 subgrid", "unit": "evals/s",
+          "fp64": v64, "mixed": vmx, "ratio": vmx / v64,
+          "mixed_lndet_rel_err_vs_fp64": {"max": float(err.max()), "median": float(np.median(err)),
+                                          "points": int(err.size)},
+          "im_branch_max_dist": float(np.max(np.abs(((omx.imag - o64.imag) * 2048 + np.pi) % (2 * np.pi) - np.pi))),
+          "status_nonzero": {"mixed": int(np.count_nonzero(smx)), "fp64": int(np.count_nonzero(s64))}}
+    if o is not None:
+        idx = np.arange(0, len(ks), len(ks) // (2 * th))[:2 * th]
+        t0 = time.perf_counter()
+        ref, _ = o.tracelog_batch(2, 2048, med.pos, ks[idx], nthreads=th)
+        el = time.perf_counter() - t0
+        c3["cpu_baseline"] = {"value": len(idx) / el, "unit": "evals/s", "cores": th, "kind": "port",
+                              "sample": f"{len(idx)} points spread over the subgrid, {th} OpenMP threads x 1 "
+                                        "OpenBLAS thread"}
+        c3["lndet_rel_err_vs_oracle"] = {
+            "fp64": float(np.max(np.abs((o64[idx] - ref).real) / np.abs(ref.real))),
+            "mixed": float(np.max(np.abs((omx[idx] - ref).real) / np.abs(ref.real))), "points": int(len(idx))}
+    legs["C3"] = c3
+    # C5: d=3 N=4096 seed 1, plane wave along +x, 256 real k in [0.5,3], psi on 512x512 pixels at z=0
+    n, nk, npx = 4096, 256, 512
+    med = ms.Medium(3, n, seed=1)
+    rad = (n / (4.0 / 3.0 * np.pi)) ** (1.0 / 3.0)
+    dom = [-rad, rad, -rad, rad]
+    ks = 0.5 + 2.5 * np.arange(nk) / (nk - 1) + 0j
+    sub = np.arange(0, nk, 16)
+    (f_m, _, _, a_m), el_m = _wall(torch, lambda: ms.wave_function_batch([med], ks, npx, npx, dom, "mixed",
+                                                                         want_psi=False))
+    (f_d, _, _, a_d), el_d = _wall(torch, lambda: ms.wave_function_batch([med], ks[sub], npx, npx, dom, "fp64",
+                                                                         want_psi=False))
+    c5 = {"workload": "wavefunction d=3 N=4096 256 real k in [0.5,3], 512x512 grid z=0", "unit": "k/s",
+          "mixed": nk / el_m, "mixed_seconds": el_m, "fp64": len(sub) / el_d, "fp64_seconds": el_d,
+          "fp64_sample": f"every 16th k ({len(sub)} of {nk}): {len(sub)} N=4096 solves on as many CTAs, "
+                         "so this rate is the latency of one FP64 solve, not the engine's throughput",
+          "fun_max_abs_diff_vs_fp64": float(np.max(np.abs(f_m[sub] - f_d))),
+          "fun_max_abs": float(np.max(np.abs(f_d))),
+          "amp_max_rel_diff_vs_fp64": float(np.max(np.abs(a_m[0][sub] - a_d[0])) / np.max(np.abs(a_d[0])))}
+    worst = {"mixed": 0.0, "fp64": 0.0}
+    for j in (0, len(sub) - 1):
+        k = ks[sub[j]]
+        m = ms.build_ms_matrix(med, k)
+        phi = np.exp(1j * k * med.pos[0::3])
+        for prec, a in (("mixed", a_m[0][sub[j]]), ("fp64", a_d[0][j])):
+            worst[prec] = max(worst[prec], float(np.max(np.abs(phi - m @ a)) / np.max(np.abs(phi))))
+    c5["solve_residual_max"] = worst
+    if o is not None:
+        t0 = time.perf_counter()
+        o.wavefunction(3, n, med.pos, ks[nk // 2], 2, 2, dom, nthreads=th)
+        t_solve = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o.wavefunction(3, n, med.pos, ks[nk // 2], 96, 96, dom, nthreads=th)
+        t_px = max(time.perf_counter() - t0 - t_solve, 0.0) / (96 * 96 - 4)
+        c5["cpu_baseline"] = {"value": 1.0 / (t_solve + t_px * npx * npx), "unit": "k/s", "cores": th,
+                              "kind": "port", "sample": f"one k: N=4096 zgesv {t_solve:.2f} s + "
+                                                        f"{t_px * 1e6:.2f} us per pixel (96x96 grid), scaled to "
+                                                        f"{npx}x{npx} pixels"}
+    legs["C5"] = c5
+    return legs
+
+
 WORKLOADS = {"map64": workload_map64, "map2d": workload_map2d, "aberth": workload_aberth, "wave": workload_wave}
 
 
@@ -554,7 +661,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg of an fp64 run")
-    ap.add_argument("--aberth", type=int, default=32, help="realisations of the resonance-search leg (0: skip)")
+    ap.add_argument("--aberth", type=int, default=256, help="realisations of the resonance-search leg (0: skip)")
+    ap.add_argument("--aberth-fp64", type=int, default=32,
+                    help="realisations of the resonance-search leg also searched in FP64")
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="weak: each GPU the whole cut of its own realisation; strong: one realisation's cut "
+                         "split over the GPUs")
+    ap.add_argument("--no-legs", dest="legs_default", action="store_false",
+                    help="skip the compact C1/C3/C5 legs of the default line")
     ap.add_argument("--workload", default="cut", choices=["cut"] + sorted(WORKLOADS),
                     help="cut: the headline line; others: one measurement line of that configuration")
     ap.add_argument("--count", type=int, default=0, help="aberth workload: realisations (default 4096)")
@@ -576,10 +690,17 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(lr)
     ms.init(lr)
-    seed = rank + 1
     natom = args.natom
-    med = ms.Medium(D, natom, seed=seed)
     ks = workload_ks()[:args.nk]
+    nk_total = len(ks)
+    if args.scaling == "strong":
+        # one realisation (seed 1), its cut split over the ranks in contiguous blocks
+        from msmodel_gb300.sharding import split_points
+        seed = 1
+        ks = ks[split_points(nk_total, rank, ws)].copy()
+    else:
+        seed = rank + 1  # weak: each rank its own realisation, the whole cut
+    med = ms.Medium(D, natom, seed=seed)
     job = ms.Job("tracelog", [med], ks, precision=args.precision)
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -607,14 +728,14 @@ def main():
             times.append(e0.elapsed_time(e1) * 1e-3)
     barrier()
     launches = ms.launch_count() - l0
-    phase_cycles = ms.engine_stats() if os.environ.get("MSGPU_STATS") else None
+    phase_cycles = ms.engine_stats() if os.environ.get("MSGPU_STATS") and args.precision == "mixed" else None
     clocks = clk.summary()
     tot = sum(times)
     if ws > 1:
         t = torch.tensor([tot], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         tot = float(t.item())
-    units = args.steps * len(ks) * ws
+    units = args.steps * (nk_total if args.scaling == "strong" else len(ks) * ws)
     value = units / tot
     out, st = job.results()
     assert np.all(st == 0), "non-zero status in the benchmark results"
@@ -656,30 +777,39 @@ def main():
     mixed = None
     if args.precision == "fp64" and not args.no_mixed:
         mixed = measure_mixed(ms, torch, med, ks, out, args, stream, flush, ws, barrier)
+        if os.environ.get("MSGPU_STATS"):
+            mixed["phase_cycles"] = ms.engine_stats()
 
     aberth = None
     if rank == 0 and args.aberth > 0 and args.precision == "fp64":
-        aberth = measure_aberth(ms, torch, args.aberth, 0 if args.no_cpu else min(args.aberth, os.cpu_count() or 1))
+        aberth = measure_aberth(ms, torch, args.aberth, args.aberth_fp64,
+                                0 if args.no_cpu else min(args.aberth, os.cpu_count() or 1))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline()
+
+    legs = None
+    if rank == 0 and args.legs_default and args.precision == "fp64":
+        legs = config_legs(ms, torch, args.no_cpu)
 
     if mixed:
         mixed["ratio_vs_fp64"] = mixed["value"] / value
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)" if args.precision == "fp64" else
+                "scaling": args.scaling, "vs_baseline": None, "dtype": "c128 (f64)" if args.precision == "fp64" else
                 "c128 in / bf16-split tensor LU",
                 "data": "synthetic (seeded scatterers drawn by the reference's generator; no dataset)",
                 "config": {"workload": f"kcut d=3 N={natom} {len(ks)}k Im=-0.05", "d": D, "natom": natom, "nk": len(ks),
                            "model": "maximum", "shape": "ball", "precision": args.precision,
-                           "parallelism": f"replicas x{ws} (one realisation per GPU)",
+                           "parallelism": (f"replicas x{ws} (one realisation per GPU)" if args.scaling == "weak"
+                                           else f"points split x{ws} (one realisation, {nk_total} k over the GPUs)"),
                            "l2": "flushed between steps (256 MB write); per-CTA working set 5 GB > L2"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches,
                 **({"mixed": mixed} if mixed else {}),
                 **({"aberth": aberth} if aberth else {}),
+                **({"configs": legs} if legs else {}),
                 **({"phase_cycles": phase_cycles} if phase_cycles else {}),
                 "precision": args.precision}
         print(json.dumps(line))

@@ -41,6 +41,9 @@ enum { MSGPU_RF_CRSEC = 0, MSGPU_RF_DOS = 1 };
 #define MSGPU_S_RANGE 4     /* mixed precision: an entry beyond the FP32-safe range (|M_ij| >= 1e18), no result */
 #define MSGPU_S_TIMEOUT 8   /* a bounded device wait gave up; the result is void */
 #define MSGPU_S_NOCONV 16   /* inverse iteration: not converged within its 50 steps (value = last estimate) */
+#define MSGPU_S_SPAN 32     /* mixed precision: the matrix entries spanned more than 2^8 but the run sliced four
+                               ways, so the 1e-8 accuracy target is not guaranteed (never set when the job's
+                               entry span was predicted correctly on the host) */
 
 /* error codes */
 #define MSGPU_E_ARG (-1)
@@ -100,7 +103,10 @@ void msgpu_halton_points(const double* dom, int n, double* z);
  *        5 = the d = 3 element M_ij = -G(k,r) and 6 = dM_ij/dk with FP64
  *            distance and reductions, double-float series (d ignored),
  *        7, 8 = the same two entirely in double-float on the FP32 pipe, as the
- *            mixed engine assembles d = 3 matrices (r rounded to 48 bits) */
+ *            mixed engine assembles d = 3 matrices (r rounded to 48 bits),
+ *        9, 10 = the d = 2 element M_ij = K_0(-ikr)/(2 pi) and dM_ij/dk in
+ *            double-float on the FP32 pipe, as the mixed engine assembles
+ *            d = 2 matrices (d ignored) */
 int msgpu_eval_special(int which, int d, const msgpu_model* model, int n, const double* ks, const double* rs,
                        double* out);
 
@@ -269,6 +275,13 @@ int msgpu_job_set_points(msgpu_job* job, int nitem, const int* item_med, const d
 int msgpu_job_use_graph(msgpu_job* job, int on);
 int msgpu_job_results(msgpu_job* job, double* out, int* status);
 int msgpu_job_amplitudes(msgpu_job* job, double* amps);
+/* Eigenvector jobs (kind 4): the starting vector of every item's inverse
+ * iteration, in the layout msgpu_job_amplitudes returns (n_i complex values
+ * per item, concatenated in item order); from then on the job starts each
+ * inverse iteration from these vectors instead of the constant unit vector,
+ * as the reference's mineigval does with the vector of its previous call
+ * (src/core/ms_core.c:339-340).  Each run overwrites them with its eigenvectors. */
+int msgpu_job_set_vectors(msgpu_job* job, const double* vecs);
 /* kernels launched by one msgpu_job_run */
 int msgpu_job_launches(const msgpu_job* job);
 /* algorithmic real flops of one msgpu_job_run (8/3 n^3 per ln det; 8/3 n^3 + 8 n^3 per dlogf) */
@@ -278,6 +291,13 @@ void msgpu_job_destroy(msgpu_job* job);
  * with the environment variable MSGPU_STATS set: out[0..6] = assembly, panel,
  * TRSM, slicing, tensor tiles, solves, items.  Returns the count written. */
 int msgpu_engine_stats(double* out, int n);
+/* Failure-path test hook, no counterpart in the reference: the poll limit of
+ * the first operand wait (an mbarrier wait on a bulk copy) of every mixed
+ * trailing update in later runs; polls < 0 restores the normal limit.  With 0
+ * that wait runs out at once: the engine issues no MMA, lets the copy in
+ * flight land, marks the item and every item not yet taken MSGPU_S_TIMEOUT
+ * (value NaN), frees its tensor memory and returns; the device stays usable. */
+int msgpu_debug_first_wait_limit(int polls);
 
 #ifdef __cplusplus
 }

@@ -76,6 +76,7 @@ def lib():
     L.msgpu_job_flops.restype = C.c_double
     L.msgpu_job_destroy.argtypes = [C.c_void_p]
     L.msgpu_engine_stats.argtypes = [_dp, C.c_int]
+    L.msgpu_debug_first_wait_limit.argtypes = [C.c_int]
     L.msgpu_wave_function.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, C.c_int, _dp, _dp, _dp, C.c_void_p,
                                        C.c_void_p, C.c_int]
     L.msgpu_wave_function_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _dp, C.c_int, C.c_int, _dp, _dp,
@@ -127,6 +128,12 @@ def engine_stats():
         return None
     names = ["assemble", "panel", "trsm", "slice", "tiles", "solve", "items"]
     return {k: float(v) for k, v in zip(names, out[:n])}
+
+
+def debug_first_wait_limit(polls):
+    """Poll limit of the first operand wait of each mixed trailing update
+    (polls < 0: the normal limit); 0 makes that wait run out (failure-path tests)."""
+    _check(lib().msgpu_debug_first_wait_limit(int(polls)), "debug_first_wait_limit")
 
 
 def sm_count():
@@ -511,6 +518,65 @@ def imag_mu_histogram(mus, nbin, xmin, xmax):
     total = counts.sum()
     dens = counts / (centres * total * np.log(xmax / xmin) / nbin) if total else counts
     return dens, centres, lost
+
+
+def chistogram(mus, xbin, ybin, mbin, dom=None, mrange=None):
+    """The mu-plane histogram of run_chistogram_omp (ms_core.c:173-232) from the
+    eigenvalues of every realisation, binned as fill_chist does
+    (chistogram_util.c:103-264):
+      * moments: the mean and the per-component standard deviation of mu;
+      * domain {xmin, xmax, ymin, ymax}: given, or the extremes of the values;
+        pixel (ix, iy) = (round((xbin-1)(Re mu - xmin)/(xmax - xmin)),
+        round((ybin-1)(ymax - Im mu)/(ymax - ymin))), row-major from the top
+        row, counts (not normalised, as the reference leaves them);
+      * marginal of Im mu on mbin log-spaced bin centres over [mmin, mmax]
+        (given, or the range of Im mu): bin round((mbin-1) ln(Im mu/mmin) /
+        ln(mmax/mmin)), normalised to unit integral with the width fac x of
+        each bin, fac = ln(mmax/mmin)/(mbin-1).
+    Values outside a range are lost (counted once per range they miss).
+    Returns dict(data[ybin, xbin], mdata[mbin], dom, mrange, avg, sigma, lost)."""
+    z = np.concatenate([np.asarray(m, dtype=np.complex128).ravel() for m in mus])
+    if z.size < 2:
+        raise ValueError("chistogram: at least two values are needed to set up the domain")
+    avg = z.mean()
+    dz = z - avg
+    sigma = complex(np.sqrt(np.mean(dz.real ** 2)), np.sqrt(np.mean(dz.imag ** 2)))
+    if dom is None:
+        dom = [float(z.real.min()), float(z.real.max()), float(z.imag.min()), float(z.imag.max())]
+    if mrange is None:
+        mrange = [float(z.imag.min()), float(z.imag.max())]
+    xmin, xmax, ymin, ymax = dom
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ix = np.round((xbin - 1) * (z.real - xmin) / (xmax - xmin))
+        iy = np.round((ybin - 1) * (ymax - z.imag) / (ymax - ymin))
+    ok = np.isfinite(ix) & np.isfinite(iy) & (ix >= 0) & (ix < xbin) & (iy >= 0) & (iy < ybin)
+    data = np.zeros(xbin * ybin)
+    np.add.at(data, (ix[ok] + iy[ok] * xbin).astype(np.int64), 1.0)
+    lost = int(z.size - ok.sum())
+    mmin, mmax = mrange
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lmin, lmax = np.log(mmin), np.log(mmax)
+        im = np.round((mbin - 1) * (np.log(z.imag) - lmin) / (lmax - lmin))
+    okm = np.isfinite(im) & (im >= 0) & (im < mbin)
+    mdata = np.zeros(mbin)
+    np.add.at(mdata, im[okm].astype(np.int64), 1.0)
+    lost += int(z.size - okm.sum())
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fac = np.log(mmax / mmin) / (mbin - 1)
+        x = mmin * np.exp(fac * np.arange(mbin))
+        mdata = mdata / (fac * x * mdata.sum())
+    return {"data": data.reshape(ybin, xbin), "mdata": mdata, "dom": dom, "mrange": mrange, "avg": complex(avg),
+            "sigma": sigma, "lost": lost}
+
+
+def run_chistogram(media, k, xbin, ybin, mbin, dom=None, mrange=None):
+    """run_chistogram_omp (ms_core.c:173-232): the eigenvalues of M(k) of every
+    realisation on the GPU (eigvals_batch), binned by chistogram."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    mus, st = eigvals_batch(media, np.full(len(media), complex(k)), np.arange(len(media), dtype=np.int32))
+    out = chistogram(mus, xbin, ybin, mbin, dom, mrange)
+    out["status"] = st
+    return out
 
 
 EIG_METHODS = {"determinant": 0, "mineigval": 1, "invtraceinv": 2}

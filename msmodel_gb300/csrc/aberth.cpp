@@ -59,7 +59,8 @@ void least_squares(int m, int nc, std::vector<cd>& a, std::vector<cd>& b) {
 
 struct Realisation {
     std::vector<cd> z;
-    std::vector<int> flag;
+    std::vector<int> flag;  // 0 in progress, 1 converged, -1 failed, 2 parked (mixed: FP64 finish pending)
+    std::vector<int> used;  // sweeps this root has taken part in
     std::vector<cd> poly;
     int nr = 0;
     bool aborted = false;
@@ -170,9 +171,22 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
             }
         }
     }
-    // One sweep over every realisation: batched dlogf of the roots in progress,
-    // then the reference's sequential update.  Returns false on a GPU error.
-    auto sweep = [&](int prec, double tol, int& err) -> bool {
+    // Mixed precision.  Near a root M is nearly singular and tr(M^-1 dM/dk)
+    // magnifies the factorisation's error by its condition number, so a root
+    // whose relative step falls below SWITCH in mixed precision is parked (the
+    // step applied) and later finished with FP64 dlogf.  A mixed step that
+    // already meets the reference's stop test |dz| < toler |z| ends the root
+    // as in the reference (the mixed dlogf is sliced six ways, ~1e-11
+    // relative, so the test decides as FP64 would).  Every root keeps the
+    // reference's budget of maxit sweeps in all (root_finder.c:545-576): the
+    // FP64 sweeps of a parked root count against the sweeps it has used, and
+    // a root still in progress when its budget is spent fails.  The
+    // Newton/Aberth update is FP64 throughout.
+    constexpr double SWITCH = 1e-7;
+    // One sweep over every realisation: batched dlogf of the roots in progress
+    // (flag 0) at precision prec, then the reference's sequential update.
+    // Returns false when no root is in progress or on a GPU error.
+    auto sweep = [&](int prec, int& err) -> bool {
         std::vector<int> im;
         std::vector<double> ks;
         for (int r = 0; r < nmed; ++r) {
@@ -196,6 +210,7 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
             Realisation& X = R[r];
             for (int i = 0; i < X.nr; ++i) {
                 if (X.flag[i] != 0) continue;
+                ++X.used[i];
                 cd pv = 0.0;
                 if (deg >= 0) {
                     pv = X.poly[deg];
@@ -206,32 +221,34 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
                 for (int j = 0; j < X.nr; ++j)
                     if (j != i) inv -= 1.0 / (X.z[i] - X.z[j]);
                 cd dz = 1.0 / inv, zn = X.z[i] - dz;
-                if (!in_dom(dom, zn)) X.flag[i] = -1;
-                else if (std::abs(dz) < tol * std::abs(X.z[i])) X.flag[i] = 1;
-                else X.z[i] = zn;
+                if (!in_dom(dom, zn)) {
+                    X.flag[i] = -1;
+                } else if (std::abs(dz) < toler * std::abs(X.z[i])) {
+                    X.flag[i] = 1;
+                } else {
+                    if (prec == MSGPU_MIXED && std::abs(dz) < SWITCH * std::abs(X.z[i])) X.flag[i] = 2;  // parked
+                    X.z[i] = zn;
+                }
             }
         }
         return true;
     };
+    for (int r = 0; r < nmed; ++r) R[r].used.assign(R[r].nr, 0);
     int err = 0;
+    for (int s = 0; s < maxit && sweep(precision, err); ++s) {
+    }
+    if (err) return err;
     if (precision == MSGPU_MIXED) {
-        // Mixed-precision dlogf loses accuracy as 1/distance to a root (M is
-        // nearly singular there): iterate in mixed precision to a relative step
-        // of 1e-7, then finish every such root with FP64 dlogf and the
-        // reference's tolerance (the Newton/Aberth update itself is FP64 all along).
-        const double tol1 = std::max(toler, 1e-7);
-        for (int s = 0; s < maxit && sweep(MSGPU_MIXED, tol1, err); ++s) {
-        }
-        if (err) return err;
+        // FP64 finish of the parked roots, each within its remaining budget
         for (int r = 0; r < nmed; ++r)
             for (int i = 0; i < R[r].nr; ++i)
-                if (R[r].flag[i] == 1) R[r].flag[i] = 0;
-                else if (R[r].flag[i] == 0) R[r].flag[i] = -1;  // did not settle in mixed precision
-        for (int s = 0; s < 8 && sweep(MSGPU_FP64, toler, err); ++s) {
-        }
-        if (err) return err;
-    } else {
-        for (int s = 0; s < maxit && sweep(precision, toler, err); ++s) {
+                if (R[r].flag[i] == 2) R[r].flag[i] = 0;
+                else if (R[r].flag[i] == 0) R[r].flag[i] = -1;  // budget spent in mixed precision
+        for (;;) {
+            for (int r = 0; r < nmed; ++r)
+                for (int i = 0; i < R[r].nr; ++i)
+                    if (R[r].flag[i] == 0 && R[r].used[i] >= maxit) R[r].flag[i] = -1;
+            if (!sweep(MSGPU_FP64, err)) break;
         }
         if (err) return err;
     }

@@ -61,13 +61,15 @@ static __device__ zc cnormalize_block(zc* __restrict__ x, int n, LuSmem& s) {
     return fac;
 }
 
-// inverse_iteration (ms_matrix_util.c:279) on the LU already in A: from the
+// inverse_iteration (ms_matrix_util.c:279) on the LU already in A: from
+// `start` (n complex values, the caller's previous eigenvector) or else the
 // constant unit vector, x <- normalize(A^-1 x) until |x - x_old| < 1e-10 or 50
 // steps (the reference's ivit_maxit / ivit_toler); returns lambda = 1 / fac,
 // the eigenvalue of smallest modulus, x the eigenvector; conv = 0 if not reached.
 static __device__ zc inverse_iteration(const zc* __restrict__ A, zc* __restrict__ x, zc* __restrict__ xold, int n,
-                                       const int* __restrict__ ipiv, LuSmem& s, int& conv) {
-    for (int i = threadIdx.x; i < n; i += NT) x[i] = mk(1.0);
+                                       const int* __restrict__ ipiv, LuSmem& s, int& conv,
+                                       const double* __restrict__ start) {
+    for (int i = threadIdx.x; i < n; i += NT) x[i] = start ? mk(start[2 * i], start[2 * i + 1]) : mk(1.0);
     __syncthreads();
     zc fac = cnormalize_block(x, n, s);
     conv = 0;
@@ -126,7 +128,8 @@ __global__ void __launch_bounds__(NT, 2) k_engine_fp64(EngineParams P) {
             res = lu_trace_solve(A, B, md.n, ipiv, s);
         } else if (P.kind == 4) {
             const size_t vec = (((size_t)P.piv_stride + 15) / 16) * 16;
-            res = inverse_iteration(A, B, B + vec, md.n, ipiv, s, conv);
+            res = inverse_iteration(A, B, B + vec, md.n, ipiv, s, conv,
+                                    P.warm && P.amps ? P.amps + 2 * P.amp_off[it] : nullptr);
             if (P.amps)
                 for (int i = threadIdx.x; i < md.n; i += NT) {
                     P.amps[2 * (P.amp_off[it] + i)] = B[i].re;
@@ -294,6 +297,11 @@ struct msgpu_job {
     double flops = 0.0;
     int grid = 0;
     std::vector<int> med_n;  // n of every medium (host copy)
+    // mixed engine: per medium the smallest and largest pair distance (d = 3 with the
+    // "maximum" model), or a negative smallest distance where the entry span is not predicted
+    std::vector<double> med_rmin, med_rmax;
+    bool wide = false;       // some item may need six-way slicing (sticky: captured graphs keep it)
+    bool warm = false;       // kind 4: inverse iterations start from the vectors set by msgpu_job_set_vectors
     bool d3only = true;      // every medium has d = 3
     MedDev* d_media = nullptr;
     double* d_pos = nullptr;
@@ -435,6 +443,31 @@ int msgpu_tracelog_matrix(int n, const double* mat, double* out, int* info) {
     return 0;
 }
 
+// Could the entries of M(k) (and of dM/dk for kind 1) of an item span more
+// than the mixed engine's four-slice budget?  For d = 3 and the "maximum"
+// model the moduli are known in closed form: off the diagonal
+// |G| = e^{a r} / (4 pi r) (a = -Im k) and |dG/dk| = e^{a r} / (4 pi) over the
+// pair distances [rmin, rmax], on the diagonal |k| / (4 pi) and 1 / (4 pi).
+// The predicted span of the moduli, times 2 sqrt 2 (the engine measures
+// max(|Re|, |Im|), within sqrt 2 of the modulus), is compared with the
+// engine's threshold; anything not covered counts as wide.
+static bool item_may_be_wide(double rmin, double rmax, int kind, double kre, double kim) {
+    if (!(rmin > 0.0) || !(rmax >= rmin)) return true;
+    const double a = -kim;
+    auto g = [&](double r) { return std::exp(a * r) / r; };  // 4 pi |G|, up to the common factor
+    double hi = std::max(g(rmin), g(rmax)), lo = std::min(g(rmin), g(rmax));
+    if (a > 0.0 && 1.0 / a > rmin && 1.0 / a < rmax) lo = std::min(lo, g(1.0 / a));
+    const double kabs = std::hypot(kre, kim);
+    hi = std::max(hi, kabs);
+    lo = std::min(lo, kabs);
+    if (kind == 1) {
+        const double e1 = std::exp(a * rmin), e2 = std::exp(a * rmax);
+        hi = std::max({hi, e1, e2, 1.0});
+        lo = std::min({lo, e1, e2, 1.0});
+    }
+    return !(hi <= lo * (256.0 / (2.0 * std::sqrt(2.0))));
+}
+
 // Items of a job: medium of each, k, the queue order (largest matrices
 // first), the amplitude offsets (kind 2), the live count.  Caller holds g_mu.
 static int set_items_locked(msgpu_job* J, int nitem, const int* item_med, const double* ks) {
@@ -446,6 +479,11 @@ static int set_items_locked(msgpu_job* J, int nitem, const int* item_med, const 
         const int mi = item_med ? item_med[i] : 0;
         if (mi < 0 || mi >= J->nmed) return set_err(MSGPU_E_ARG, "job: bad item medium");
         med_of[i] = mi;
+        // dlogf jobs always slice six ways (near a root M is ill-conditioned and tr(M^-1 dM/dk)
+        // magnifies the factorisation's error by its condition number)
+        if (J->precision == MSGPU_MIXED && !J->wide)
+            J->wide = J->kind == 1 ||
+                      item_may_be_wide(J->med_rmin[mi], J->med_rmax[mi], J->kind, ks[2 * i], ks[2 * i + 1]);
         const double n = J->med_n[mi], n3 = n * n * n, n2 = n * n;
         flops += (J->kind == 0) ? 8.0 / 3.0 * n3
                  : (J->kind == 1 || J->kind == 3) ? (8.0 / 3.0 + 8.0) * n3
@@ -507,6 +545,28 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
         if (m.d != 3) J->d3only = false;
         npos += (size_t)m.n * m.d;
     }
+    // the engine that serves the job (the tuning table may hand a mixed request to the FP64 engine)
+    const TuneEntry te = kind < 3 ? g_tune[kind][precision][size_bucket(J->nmax)] : TuneEntry{};
+    if (te.engine) J->precision = te.engine - 1;
+    // pair-distance range of every d = 3 "maximum" medium (mixed jobs: the entry span of M(k))
+    J->med_rmin.assign(nmed, -1.0);
+    J->med_rmax.assign(nmed, -1.0);
+    if (J->precision == MSGPU_MIXED && kind <= 2)
+        for (int i = 0; i < nmed; i++) {
+            const msgpu_medium& m = media[i];
+            if (m.d != 3 || m.model.type != MSGPU_MAXIMUM || m.n < 2) continue;
+            double lo = INFINITY, hi = 0.0;
+            for (int a = 0; a < m.n; a++)
+                for (int b = a + 1; b < m.n; b++) {
+                    const double dx = m.pos[3 * a] - m.pos[3 * b], dy = m.pos[3 * a + 1] - m.pos[3 * b + 1],
+                                 dz = m.pos[3 * a + 2] - m.pos[3 * b + 2];
+                    const double r2 = dx * dx + dy * dy + dz * dz;
+                    lo = std::min(lo, r2);
+                    hi = std::max(hi, r2);
+                }
+            J->med_rmin[i] = std::sqrt(lo);
+            J->med_rmax[i] = std::sqrt(hi);
+        }
     auto fail = [&](const char* what) -> msgpu_job* {
         set_err(MSGPU_E_CUDA, std::string("job: ") + what);
         msgpu_job_destroy(J);
@@ -545,8 +605,6 @@ msgpu_job* msgpu_job_create(int kind, int nmed, const msgpu_medium* media, int n
     // per-CTA slots
     J->slot = (size_t)J->nmax * J->nmax;
     const size_t per_cta = slot_elems(kind, J->slot, J->nmax) * sizeof(zc);
-    const TuneEntry te = kind < 3 ? g_tune[kind][precision][size_bucket(J->nmax)] : TuneEntry{};
-    if (te.engine) J->precision = te.engine - 1;
     const int ctas = te.ctas ? std::min(te.ctas, g_ctas_fp64) : g_ctas_fp64;
     int grid = std::min(nitem, g_sms * ctas);
     size_t budget = ws_budget();
@@ -592,6 +650,8 @@ static int launch_locked(msgpu_job* J, void* ws, cudaStream_t st) {
     P.status = J->d_status;
     P.counter = J->d_counter;
     P.kind = J->kind;
+    P.wide_ok = J->wide ? 1 : 0;
+    P.warm = J->warm ? 1 : 0;
     P.amps = J->d_amps;
     P.amp_off = J->d_amp_off;
     if (J->precision == MSGPU_MIXED) {
@@ -616,7 +676,10 @@ int msgpu_job_run(msgpu_job* J, void* stream) {
         return 0;
     }
     if (J->precision == MSGPU_MIXED && mixed_prepare(J->grid, J->nmax)) return set_err(MSGPU_E_CUDA, "mixed scratch");
-    const unsigned long long gen = g_ws_gen * 0x9E3779B97F4A7C15ULL + mixed_generation();
+    // the graph holds the workspace and scratch addresses, the launch's shared-memory size
+    // (wide) and the start-vector mode (warm)
+    const unsigned long long gen =
+        ((g_ws_gen * 0x9E3779B97F4A7C15ULL + mixed_generation()) * 2 + (J->wide ? 1 : 0)) * 2 + (J->warm ? 1 : 0);
     if (!J->gexec || J->gen != gen) {
         // (re)capture: the graph holds the workspace and scratch addresses
         if (J->gexec) cudaGraphExecDestroy(J->gexec);
@@ -659,6 +722,15 @@ int msgpu_job_amplitudes(msgpu_job* J, double* amps) {
         return set_err(MSGPU_E_ARG, "job_amplitudes: not an amplitude or eigenvector job");
     CK(cudaDeviceSynchronize());
     CK(cudaMemcpy(amps, J->d_amps, sizeof(double) * 2 * (size_t)J->amp_total, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int msgpu_job_set_vectors(msgpu_job* J, const double* vecs) {
+    if (!J || J->kind != 4 || !vecs || !J->d_amps)
+        return set_err(MSGPU_E_ARG, "job_set_vectors: not an eigenvector job");
+    std::lock_guard<std::mutex> lk(g_mu);
+    CK(cudaMemcpy(J->d_amps, vecs, sizeof(double) * 2 * (size_t)J->amp_total, cudaMemcpyHostToDevice));
+    J->warm = true;
     return 0;
 }
 

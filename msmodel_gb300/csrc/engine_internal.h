@@ -29,6 +29,8 @@ struct EngineParams {
     int kind;             // 0 ln det / n, 1 dlogf, 2 amplitudes a = M^-1 phi, 3 traceinv, 4 inverse iteration
     double* amps;         // kinds 2, 4: a (or the eigenvector) per item (2 * n_i doubles each) or nullptr
     const long long* amp_off;  // kind 2: offset (in complex elements) of item i in amps
+    int wide_ok;          // mixed engine: the launch has the shared memory for six-way slicing
+    int warm;             // kind 4: start each inverse iteration from the item's vector in amps
 };
 
 
@@ -39,7 +41,8 @@ int record_error(int code, const char* what);
 
 // Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
 // negative MSGPU_E* code on error.
-// d3only: every medium of the job has d = 3 (selects the d = 3 kernel instantiation).
+// d3only: every medium of the job has d = 3 (selects the d = 3 kernel instantiation);
+// P.wide_ok: launch with the shared memory for six-way slicing.
 int mixed_run(const EngineParams& P, int grid, int nmax, bool d3only, cudaStream_t st);
 // Allocates the mixed engine's scratch for `grid` CTAs and matrices up to nmax
 // (mixed_run does so itself; called before a stream capture, which must not allocate).

@@ -14,9 +14,11 @@ uint8_t* g_img = nullptr;
 size_t g_img_bytes = 0;
 int* g_err = nullptr;
 unsigned long long* g_stats = nullptr;
+int g_first_wait = WAIT_LIMIT;
 }  // namespace
 
-static size_t mixed_smem() { return sizeof(MixSmem) + 1024; }
+// the operand buffers need 16-byte alignment (no-swizzle layout); 128 is kept
+static size_t mixed_smem() { return MIX_SMEM_WIDE; }
 
 using Variant = int (*)(const EngineParams&, const MixScratch&, int, size_t, cudaStream_t, bool);
 const Variant kVariants[6] = {mixed_variant_0_d3, mixed_variant_1_d3, mixed_variant_2_d3,
@@ -33,11 +35,12 @@ static int prepare_locked(int grid, int nmax, MixScratch& X) {
             if (f(EngineParams{}, MixScratch{}, 0, (size_t)sm, nullptr, true)) return MSGPU_E_CUDA;
         attr = true;
     }
-    const int nbA = (nmax + MT_M - 1) / MT_M, nbB = (nmax + MT_N - 1) / MT_N;
-    X.a_stride = (size_t)nbA * A_BAND;
-    X.b_stride = (size_t)nbB * B_BAND;
-    X.e_stride = (size_t)nbA * MT_M + MT_N;
-    const size_t need = (size_t)grid * (X.a_stride + X.b_stride) + 2 * sizeof(int) * grid * X.e_stride + 256;
+    // images sized for the larger of the two slice configurations
+    const int nbA = (nmax + MT_M - 1) / MT_M, ncB = (nmax + 31) / 32 * 32;
+    X.a_stride = (size_t)nbA * A_IMG_BAND;
+    X.b_stride = (size_t)ncB * B_IMG_COL;
+    X.e_stride = (size_t)nbA * MT_M + 32;
+    const size_t need = (size_t)grid * (X.a_stride + X.b_stride) + 2 * sizeof(float) * grid * X.e_stride + 256;
     if (need > g_img_bytes) {
         if (g_img) cudaFree(g_img);
         g_img = nullptr;
@@ -56,10 +59,11 @@ static int prepare_locked(int grid, int nmax, MixScratch& X) {
     }
     X.imgA = g_img;
     X.imgB = g_img + (size_t)grid * X.a_stride;
-    X.ea = reinterpret_cast<int*>(X.imgB + (size_t)grid * X.b_stride);
+    X.ea = reinterpret_cast<float*>(X.imgB + (size_t)grid * X.b_stride);
     X.eb = X.ea + (size_t)grid * X.e_stride;
     X.err = g_err;
     X.stats = getenv("MSGPU_STATS") ? g_stats : nullptr;
+    X.first_wait = g_first_wait;
     return 0;
 }
 
@@ -82,7 +86,7 @@ int mixed_run(const EngineParams& P, int grid, int nmax, bool d3only, cudaStream
     if (cudaMemsetAsync(P.counter, 0, sizeof(unsigned), st) != cudaSuccess) return MSGPU_E_CUDA;
     // variants: kinds 0..2 for media all of d = 3, then for any dimension
     const int v = (d3only ? 0 : 3) + (P.kind < 0 ? 0 : P.kind > 2 ? 2 : P.kind);
-    return kVariants[v](P, X, grid, mixed_smem(), st, false);
+    return kVariants[v](P, X, grid, P.wide_ok ? MIX_SMEM_WIDE : MIX_SMEM_NARROW, st, false);
 }
 
 int mixed_stats(double* out, int n) {
@@ -148,6 +152,16 @@ __global__ void __launch_bounds__(128, 1) k_probe_umma(const float* A, const flo
 }
 
 }  // namespace msg
+
+// Poll limit of the first operand wait of every mixed trailing update in later
+// runs (polls < 0: the normal limit).  A test sets 0 to make that wait run out
+// and checks that the items report MSGPU_S_TIMEOUT and the context stays usable.
+extern "C" int msgpu_debug_first_wait_limit(int polls) {
+    std::lock_guard<std::mutex> lk(msg::g_mx);
+    msg::g_first_wait = polls < 0 ? msg::WAIT_LIMIT : polls;
+    ++msg::g_mix_gen;  // captured runs hold the old limit: recapture them
+    return 0;
+}
 
 extern "C" int msgpu_probe_umma(int mode, const float* A, const float* B, float* D) {
     using namespace msg;

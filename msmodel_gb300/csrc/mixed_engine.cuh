@@ -12,23 +12,27 @@
 //
 // Trailing update C -= A B (A: m x K panel, B: K x nn rows, K <= 32, complex):
 //  * every row of A (column of B) is scaled by a power of two so its largest
-//    |Re|, |Im| lies in [1/2, 1), then cut into four integer slices
-//    x 2^(8-e) = s0 + s1 2^-9 + s2 2^-18 + s3 2^-27 (|s_k| <= 256); slice k is
-//    stored as the bf16 value s_k 2^-9k, which is exact (35 bits in all);
-//  * level l = i + j of a slice pair (i, j) is accumulated in its own TMEM
-//    accumulator for l = 0 and l = 1 and in a shared one for l = 2, 3: levels
-//    0 and 1 are sums of integers (in units of 2^-9l) below 2^24 and hence
-//    exact whatever order and rounding the tensor core's FP32 adder uses;
-//    the rest carries ~2^-40 of the leading term.  A numerical study of the
-//    Foldy-Lax matrices (d = 3, N <= 1024, Im k >= -1; d = 2 with moderate
-//    Im k) put ln det within ~3e-9 of FP64 with 4 slices; entries spanning
-//    more than ~1e5 within a row (d = 2 far below the real axis) lose
-//    accuracy (up to ~1e-5 at d = 2, N = 2048, Im k = -0.3), since the
-//    scale is per row;
+//    |Re|, |Im| lies in [1/2, 1), then cut into NS integer slices
+//    x 2^(8-e) = s0 + s1 2^-9 + ... + s_{NS-1} 2^-9(NS-1) (|s_k| <= 256);
+//    slice k is stored as the bf16 value s_k 2^-9k, which is exact (NS = 4:
+//    35 bits; NS = 6: 53 bits, the whole double-float);
+//  * the slice pairs (i, j) with i + j < NS are multiplied; level l = i + j is
+//    accumulated in its own TMEM accumulator for l < NG - 1 and the rest in
+//    one shared accumulator.  Levels below NG - 1 are sums of at most
+//    3 x 64 integer products below 2^16, hence integers below 2^24 and exact
+//    whatever order and rounding the tensor core's FP32 adder uses;
+//  * the slice count is chosen per item from the span of its matrix entries
+//    (largest over smallest |entry|): NS = 4 (tile 128 x 32, NG = 3) while the
+//    span is below 2^8, else NS = 6 (tile 128 x 16, NG = 4); dlogf items
+//    always take six.  The per-row scale makes the error of a product grow
+//    with the spread of magnitudes inside a row of L or a column of U: at
+//    d = 3, Im k = -0.05, N = 1024 (span 2^6) four slices keep ln det within
+//    ~1.4e-9 of FP64, while at d = 2, Im k = -0.3, N = 2048 (span 2^19, the
+//    exponential growth e^{|Im k| r} over a disk of radius 25) they leave
+//    ~1e-5 and six slices are needed;
 //  * complex = 4 real products, Re uses the negate-B bit of the instruction
-//    descriptor: 40 tcgen05.mma (128 x 32 x 16) per K-step into six TMEM
-//    accumulators (3 levels x Re/Im, 192 columns);
-//  * epilogue: C (double-float, global) -= 2^(ea+eb-16) (L0 + L1 + L23).
+//    descriptor; the accumulators use 2 NG TN TMEM columns (192 or 128);
+//  * epilogue: C (double-float, global) -= 2^(ea+eb-16) (sum of the levels).
 // Operand slices are written to global images in the tensor core's
 // core-matrix layout and moved to shared memory by bulk copies (TMA engine).
 #include <cuda_bf16.h>
@@ -40,17 +44,30 @@
 #include "df.cuh"
 #include "umma.cuh"
 #include "green_df.cuh"
+#include "green_df2.cuh"
 
 namespace msg {
 
 constexpr int MT_M = 128;               // tile rows = TMEM lanes
-constexpr int MT_N = 32;                // tile columns
 constexpr int A_SUB = MT_M * NB * 2;    // one 128 x 32 bf16 operand tile: 8 KB
-constexpr int B_SUB = MT_N * NB * 2;    // one 32 x 32 bf16 operand tile: 2 KB
-constexpr int A_BAND = 8 * A_SUB;       // 4 slices x {Re, Im}: 64 KB
-constexpr int B_BAND = 8 * B_SUB;       // 16 KB
-constexpr int TMEM_COLS = 256;          // 6 accumulators x 32 columns (allocation rounded to 2^k)
+constexpr int TMEM_COLS = 256;          // accumulators: 2 NG TN <= 192 columns (allocation rounded to 2^k)
 constexpr float RANGE_LIMIT = 1.0e18f;  // larger entries leave the safe FP32 exponent range
+constexpr float SPAN_WIDE = 256.0f;     // entry span above which an item is sliced six ways
+
+// slice configurations: NS slices per operand, TN tile columns, NG TMEM accumulator groups
+template <int NS> struct SliceCfg;
+template <> struct SliceCfg<4> { static constexpr int TN = 32, NG = 3; };
+template <> struct SliceCfg<6> { static constexpr int TN = 16, NG = 4; };
+template <int NS> __host__ __device__ constexpr int a_band() { return 2 * NS * A_SUB; }  // NS slices x {Re, Im}
+template <int NS> __host__ __device__ constexpr int b_sub() { return SliceCfg<NS>::TN * NB * 2; }
+template <int NS> __host__ __device__ constexpr int b_band() { return 2 * NS * b_sub<NS>(); }
+// shared-memory operand buffer: A band then B band (NS = 4: 64 + 16 KB; NS = 6: 96 + 12 KB)
+constexpr int GEMM_BYTES = a_band<6>() + b_band<6>() > a_band<4>() + b_band<4>() ? a_band<6>() + b_band<6>()
+                                                                                   : a_band<4>() + b_band<4>();
+// global image bytes per 128 rows of A and per column of B, the larger of the two configurations
+constexpr int A_IMG_BAND = a_band<6>();
+constexpr int B_IMG_COL = b_band<6>() / SliceCfg<6>::TN > b_band<4>() / SliceCfg<4>::TN
+                              ? b_band<6>() / SliceCfg<6>::TN : b_band<4>() / SliceCfg<4>::TN;
 
 // per-phase cycle accounting (thread 0, only when X.stats is set)
 enum { PH_ASSEMBLE = 0, PH_PANEL, PH_TRSM, PH_SLICE, PH_TILES, PH_SOLVE, PH_ITEMS, PH_N };
@@ -59,28 +76,27 @@ struct MixPanel {
     float4 T[NB][NB + 1];
     float4 T2[NB][NB + 1];
     float4 urow[NB];
-    // assembly of d = 3: sin/cos/2^x tables, coordinates of the tile's atoms as double-floats
+    // assembly of d = 3 and d = 2: sin/cos/2^x tables, coordinates of the tile's atoms as
+    // double-floats, and (d = 2) the item's K_nu constants
     Df3Tables tab;
     float4 ci[NB], cj[NB];  // x.h x.l y.h y.l
     float2 ciz[NB], cjz[NB];
+    Df2Item d2;
     // assembly of d != 3: pair lists of the K_nu regime grouping
     unsigned short list[3 * 1024];
     int cnt[4];
 };
 struct MixGemm {
-    uint8_t A[A_BAND];
-    uint8_t B[B_BAND];
+    uint8_t buf[GEMM_BYTES];  // A band at 0, B band at a_band<NS>()
 };
+// The operand buffers come last: a launch that never slices six ways (no item
+// of its job can need it) allocates only the four-slice part of the union and
+// leaves the rest of the SM's 256 KB of shared memory to the L1 cache.
 struct MixSmem {
-    union {
-        MixGemm g;
-        MixPanel p;
-    } u;
-    int ea[MT_M];
-    int eb[MT_N];
     uint64_t bar_a, bar_b, bar_mma;
     uint32_t tmem;
     int err;
+    int mma_stuck;        // an MMA completion wait ran out: 1 + the parity it waited on
     zc diag[2];
     double red_v[NT / 32];
     int red_i[NT / 32];
@@ -90,7 +106,16 @@ struct MixSmem {
     int info, bcast_i, item;
     unsigned long long stat[PH_N];
     long long t0;
+    union alignas(128) {
+        MixGemm g;
+        MixPanel p;
+    } u;
 };
+// dynamic shared memory of a launch with and without room for six slices
+constexpr size_t MIX_SMEM_WIDE = sizeof(MixSmem) + 128;
+constexpr size_t MIX_SMEM_NARROW =
+    offsetof(MixSmem, u) + (sizeof(MixPanel) > (size_t)(a_band<4>() + b_band<4>()) ? sizeof(MixPanel)
+                                                                                     : (size_t)(a_band<4>() + b_band<4>())) + 128;
 
 __device__ __forceinline__ void stat_start(MixSmem& s) {
     if (threadIdx.x == 0) s.t0 = clock64();
@@ -105,13 +130,15 @@ __device__ __forceinline__ void stat_add(MixSmem& s, int ph) {
 
 // per-CTA global scratch of the mixed engine
 struct MixScratch {
-    uint8_t* imgA;   // ceil(nmax/128) * A_BAND per CTA
-    uint8_t* imgB;   // ceil(nmax/64) * B_BAND per CTA
-    int* ea;         // exponents, padded
-    int* eb;
+    uint8_t* imgA;   // ceil(nmax/128) * A_IMG_BAND per CTA
+    uint8_t* imgB;   // (ceil(nmax/32) * 32) * B_IMG_COL per CTA
+    float* ea;       // row and column scales 2^(e-8) of the sliced operands, padded
+    float* eb;
     size_t a_stride, b_stride, e_stride;
     int* err;        // device flag: 1 = an mbarrier wait timed out
     unsigned long long* stats;  // per-phase SM cycles summed over CTAs, or nullptr
+    int first_wait;  // poll limit of the first operand wait of each trailing update (WAIT_LIMIT
+                     // unless a test shortens it to make that wait run out)
 };
 
 
@@ -120,17 +147,18 @@ struct Phases {
 };
 
 // ---------------------------------------------------------------- slicing
-// four pre-scaled bf16 slices of the double-float x (hi, lo) for row exponent e:
-// x 2^(8-e) = s0 + s1 2^-9 + s2 2^-18 + s3 2^-27 with integers |s_k| <= 256
-// (bf16 holds every integer up to 256 exactly); 35 significant bits
-__device__ __forceinline__ void slice4(float h, float l, int e, float* o) {
+// NS pre-scaled bf16 slices of the double-float x (hi, lo) for row exponent e:
+// x 2^(8-e) = s0 + s1 2^-9 + ... with integers |s_k| <= 256 (bf16 holds every
+// integer up to 256 exactly); 8 + 9 (NS - 1) significant bits
+template <int NS>
+__device__ __forceinline__ void slice_n(float h, float l, int e, float* o) {
     float xh = ldexpf(h, 8 - e), xl = ldexpf(l, 8 - e);
     float s0 = rintf(xh);
     df r = two_sum(__fsub_rn(xh, s0), xl);
     o[0] = s0;
     float sc = 1.0f / 512.0f;
 #pragma unroll
-    for (int k = 1; k < 4; ++k) {
+    for (int k = 1; k < NS; ++k) {
         float rh = __fmul_rn(r.h, 512.0f), rl = __fmul_rn(r.l, 512.0f);
         float sk = rintf(rh);
         r = two_sum(__fsub_rn(rh, sk), rl);
@@ -150,9 +178,9 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// One operand row of K <= 32 complex values (stride `st` in float4) -> the 8
-// sub-tiles (slice k, Re/Im) of a band of R rows, row r; exponent returned.
-template <int R>
+// One operand row of K <= 32 complex values (stride `st` in float4) -> the
+// 2 NS sub-tiles (slice k, Re/Im) of a band of R rows, row r; exponent returned.
+template <int R, int NS>
 __device__ __forceinline__ int slice_operand_row(const float4* __restrict__ src, size_t st, int K, uint8_t* band, int r) {
     float mx = 0.0f;
     for (int kk = 0; kk < K; ++kk) {
@@ -162,129 +190,149 @@ __device__ __forceinline__ int slice_operand_row(const float4* __restrict__ src,
     const int e = row_exponent(mx);
     constexpr int SUB = R * NB * 2;
     for (int kb = 0; kb < NB / 8; ++kb) {
-        uint32_t w[8][4];
+        uint32_t w[2 * NS][4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            float re[2][4], im[2][4];
+            float re[2][NS], im[2][NS];
 #pragma unroll
             for (int t = 0; t < 2; ++t) {
                 const int kk = kb * 8 + 2 * q + t;
                 if (kk < K) {
                     float4 v = src[kk * st];
-                    slice4(v.x, v.y, e, re[t]);
-                    slice4(v.z, v.w, e, im[t]);
+                    slice_n<NS>(v.x, v.y, e, re[t]);
+                    slice_n<NS>(v.z, v.w, e, im[t]);
                 } else {
 #pragma unroll
-                    for (int s = 0; s < 4; ++s) re[t][s] = im[t][s] = 0.0f;
+                    for (int sl = 0; sl < NS; ++sl) re[t][sl] = im[t][sl] = 0.0f;
                 }
             }
 #pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                w[2 * s][q] = pack2(re[0][s], re[1][s]);
-                w[2 * s + 1][q] = pack2(im[0][s], im[1][s]);
+            for (int sl = 0; sl < NS; ++sl) {
+                w[2 * sl][q] = pack2(re[0][sl], re[1][sl]);
+                w[2 * sl + 1][q] = pack2(im[0][sl], im[1][sl]);
             }
         }
         const uint32_t off = cm_offset(r, kb * 8, R);
 #pragma unroll
-        for (int sub = 0; sub < 8; ++sub)
+        for (int sub = 0; sub < 2 * NS; ++sub)
             *reinterpret_cast<uint4*>(band + sub * SUB + off) = make_uint4(w[sub][0], w[sub][1], w[sub][2], w[sub][3]);
     }
     return e;
 }
 
-// A operand: rows [0, m) of the m x K panel P (column-major, ld), all bands
-static __device__ void slice_panel_rows(const float4* __restrict__ P, int ld, int m, int K, uint8_t* img, int* ea) {
+// A operand: rows [0, m) of the m x K panel P (column-major, ld), all bands;
+// ea[i] = 2^(e_i - 8), the row's scale
+template <int NS>
+static __device__ void slice_panel_rows(const float4* __restrict__ P, int ld, int m, int K, uint8_t* img, float* ea) {
     const int mp = (m + MT_M - 1) / MT_M * MT_M;
     for (int i = threadIdx.x; i < mp; i += NT) {
-        uint8_t* band = img + (size_t)(i / MT_M) * A_BAND;
+        uint8_t* band = img + (size_t)(i / MT_M) * a_band<NS>();
         const int r = i % MT_M;
         if (i < m) {
-            ea[i] = slice_operand_row<MT_M>(P + i, (size_t)ld, K, band, r);
+            ea[i] = ldexpf(1.0f, slice_operand_row<MT_M, NS>(P + i, (size_t)ld, K, band, r) - 8);
         } else {
-            ea[i] = 0;
+            ea[i] = 0.0f;
             for (int kb = 0; kb < NB / 8; ++kb)
-                for (int sub = 0; sub < 8; ++sub)
+                for (int sub = 0; sub < 2 * NS; ++sub)
                     *reinterpret_cast<uint4*>(band + sub * A_SUB + cm_offset(r, kb * 8, MT_M)) = make_uint4(0, 0, 0, 0);
         }
     }
 }
 
-// B operand: columns [0, nn) of the K x nn block Bp (column-major, ld)
-static __device__ void slice_block_cols(const float4* __restrict__ Bp, int ld, int nn, int K, uint8_t* img, int* eb) {
-    const int np = (nn + MT_N - 1) / MT_N * MT_N;
+// B operand: columns [0, nn) of the K x nn block Bp (column-major, ld); eb[j] = 2^(e_j - 8)
+template <int NS>
+static __device__ void slice_block_cols(const float4* __restrict__ Bp, int ld, int nn, int K, uint8_t* img, float* eb) {
+    constexpr int TN = SliceCfg<NS>::TN;
+    const int np = (nn + TN - 1) / TN * TN;
     for (int j = threadIdx.x; j < np; j += NT) {
-        uint8_t* band = img + (size_t)(j / MT_N) * B_BAND;
-        const int r = j % MT_N;
+        uint8_t* band = img + (size_t)(j / TN) * b_band<NS>();
+        const int r = j % TN;
         if (j < nn) {
-            eb[j] = slice_operand_row<MT_N>(Bp + (size_t)j * ld, 1, K, band, r);
+            eb[j] = ldexpf(1.0f, slice_operand_row<TN, NS>(Bp + (size_t)j * ld, 1, K, band, r) - 8);
         } else {
-            eb[j] = 0;
+            eb[j] = 0.0f;
             for (int kb = 0; kb < NB / 8; ++kb)
-                for (int sub = 0; sub < 8; ++sub)
-                    *reinterpret_cast<uint4*>(band + sub * B_SUB + cm_offset(r, kb * 8, MT_N)) = make_uint4(0, 0, 0, 0);
+                for (int sub = 0; sub < 2 * NS; ++sub)
+                    *reinterpret_cast<uint4*>(band + sub * b_sub<NS>() + cm_offset(r, kb * 8, TN)) =
+                        make_uint4(0, 0, 0, 0);
         }
     }
 }
 
 // ---------------------------------------------------------------- tensor-core update
-// Accumulators (TMEM columns 32 a .. 32 a + 31), one per slice level so that
-// levels 0 and 1 stay exact whatever the tensor core's FP32 summation order
-// and rounding: a = 0/1 level 0 (Re/Im), 2/3 level 1, 4/5 levels 2 and 3.
-__device__ __forceinline__ void issue_tile_mmas(MixSmem& s, uint32_t tmem) {
-    const uint32_t idp = idesc_bf16(MT_M, MT_N, false, false), idn = idesc_bf16(MT_M, MT_N, false, true);
-    const uint32_t a0 = smem_u32(s.u.g.A), b0 = smem_u32(s.u.g.B);
-    // core-matrix strides: K direction (LBO) R/8*128, row direction (SBO) 128
-    auto dA = [&](int k, int c, int ks) { return sdesc(a0 + (k * 2 + c) * A_SUB + ks * 4096, 2048, 128); };
-    auto dB = [&](int k, int c, int ks) { return sdesc(b0 + (k * 2 + c) * B_SUB + ks * 1024, 512, 128); };
-    // slice pairs (i, j) and their accumulator group
-    constexpr int NP = 10;
-    const int PI[NP] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-    const int PJ[NP] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
-    const int PG[NP] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2};
+// Accumulator group g (TMEM columns 2 TN g .. +TN for Re, +TN .. +2 TN for Im)
+// holds slice level l = g for g < NG - 1 and levels >= NG - 1 in the last
+// group, so that the low levels stay exact whatever the tensor core's FP32
+// summation order and rounding.
+template <int NS>
+__device__ __forceinline__ void issue_tile_mmas(uint32_t a0, uint32_t b0, uint64_t* bar, uint32_t tmem) {
+    constexpr int TN = SliceCfg<NS>::TN, NG = SliceCfg<NS>::NG, BSUB = b_sub<NS>();
+    const uint32_t idp = idesc_bf16(MT_M, TN, false, false), idn = idesc_bf16(MT_M, TN, false, true);
+    // core-matrix strides: K direction (LBO) R/8*128, row direction (SBO) 128; a K step of 16 is R*32 bytes
+    auto dA = [&](int k, int c, int ks) { return sdesc(a0 + (k * 2 + c) * A_SUB + ks * (MT_M * 32), MT_M * 16, 128); };
+    auto dB = [&](int k, int c, int ks) { return sdesc(b0 + (k * 2 + c) * BSUB + ks * (TN * 32), TN * 16, 128); };
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            const bool first_of_group = (p == 0 || PG[p - 1] != PG[p]);
-            const uint32_t acc = (ks > 0 || !first_of_group) ? 1u : 0u;
-            const uint32_t tre = tmem + 64 * PG[p], tim = tre + 32;
-            umma_bf16(tre, dA(PI[p], 0, ks), dB(PJ[p], 0, ks), idp, acc);
-            umma_bf16(tre, dA(PI[p], 1, ks), dB(PJ[p], 1, ks), idn, 1);
-            umma_bf16(tim, dA(PI[p], 0, ks), dB(PJ[p], 1, ks), idp, acc);
-            umma_bf16(tim, dA(PI[p], 1, ks), dB(PJ[p], 0, ks), idp, 1);
+        for (int l = 0; l < NS; ++l) {
+            const int g = l < NG - 1 ? l : NG - 1;
+#pragma unroll
+            for (int i = 0; i <= l; ++i) {
+                const int j = l - i;
+                const uint32_t acc = (ks == 0 && i == 0 && l == g) ? 0u : 1u;  // first product of group g
+                const uint32_t tre = tmem + 2 * TN * g, tim = tre + TN;
+                umma_bf16(tre, dA(i, 0, ks), dB(j, 0, ks), idp, acc);
+                umma_bf16(tre, dA(i, 1, ks), dB(j, 1, ks), idn, 1);
+                umma_bf16(tim, dA(i, 0, ks), dB(j, 1, ks), idp, acc);
+                umma_bf16(tim, dA(i, 1, ks), dB(j, 0, ks), idp, 1);
+            }
         }
     }
-    umma_commit(&s.bar_mma);
+    umma_commit(bar);
 }
 
-__device__ __forceinline__ df df_sub_levels(df c, float l0, float l1, float l23) {
-    const df s = two_sum(c.h, -l0);
-    const df t = two_sum(s.h, -l1);
-    const float lo = __fsub_rn(__fadd_rn(__fadd_rn(s.l, t.l), c.l), l23);
+// c - (L0 + L1 + ... ): the exact levels enter by two-sums, the last group and
+// every error term gather in one FP32 accumulator, one renormalisation
+template <int NG>
+__device__ __forceinline__ df df_sub_levels(df c, const float* lv) {
+    df t = two_sum(c.h, -lv[0]);
+    float lo = __fadd_rn(c.l, t.l);
+#pragma unroll
+    for (int g = 1; g < NG - 1; ++g) {
+        const df u = two_sum(t.h, -lv[g]);
+        lo = __fadd_rn(lo, u.l);
+        t.h = u.h;
+    }
+    lo = __fsub_rn(lo, lv[NG - 1]);
     return quick_two_sum(t.h, lo);
 }
 
 // C[m x nn] -= Ap[m x K] * Bp[K x nn]; all double-float complex, column-major.
 // tri != 0: only tiles holding an element with row >= column are updated.
 // Returns false if a wait timed out (the engine then stops).
+template <int NS>
 static __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const float4* __restrict__ Ap, int lda,
                                const float4* __restrict__ Bp, int ldb, int m, int nn, int K, int tri, MixSmem& s,
                                const MixScratch& X, uint32_t tmem, Phases& ph) {
+    constexpr int TN = SliceCfg<NS>::TN, NG = SliceCfg<NS>::NG, AB = a_band<NS>(), BB = b_band<NS>();
+    constexpr int CW = TN / 2;  // columns of a tile per thread (two warps per TMEM lane quadrant)
     if (m <= 0 || nn <= 0 || K <= 0) return true;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t* imgA = X.imgA + (size_t)blockIdx.x * X.a_stride;
     uint8_t* imgB = X.imgB + (size_t)blockIdx.x * X.b_stride;
-    int* gea = X.ea + (size_t)blockIdx.x * X.e_stride;
-    int* geb = X.eb + (size_t)blockIdx.x * X.e_stride;
+    float* gea = X.ea + (size_t)blockIdx.x * X.e_stride;
+    float* geb = X.eb + (size_t)blockIdx.x * X.e_stride;
+    uint8_t* sA = s.u.g.buf;
+    uint8_t* sB = s.u.g.buf + AB;
     stat_start(s);
-    slice_panel_rows(Ap, lda, m, K, imgA, gea);
-    slice_block_cols(Bp, ldb, nn, K, imgB, geb);
+    slice_panel_rows<NS>(Ap, lda, m, K, imgA, gea);
+    slice_block_cols<NS>(Bp, ldb, nn, K, imgB, geb);
     fence_proxy_async_all();
     __syncthreads();
     stat_add(s, PH_SLICE);
-    const int nbi = (m + MT_M - 1) / MT_M, nbj = (nn + MT_N - 1) / MT_N;
+    const int nbi = (m + MT_M - 1) / MT_M, nbj = (nn + TN - 1) / TN;
     // tile list in row-band order, skipping tiles wholly above the diagonal when tri
-    auto tile_ok = [&](int bi, int bj) { return !tri || bi * MT_M + MT_M - 1 >= bj * MT_N; };
+    auto tile_ok = [&](int bi, int bj) { return !tri || bi * MT_M + MT_M - 1 >= bj * TN; };
     auto next_tile = [&](int& bi, int& bj) {
         do {
             if (++bj >= nbj) { bj = 0; ++bi; }
@@ -294,76 +342,89 @@ static __device__ bool mixed_gemm_sub(float4* __restrict__ C, int ldc, const flo
     if (!tile_ok(bi, bj)) next_tile(bi, bj);
     if (bi >= nbi) return true;
     if (tid == 0) {
-        mbar_arrive_expect_tx(&s.bar_a, A_BAND);
-        bulk_g2s(s.u.g.A, imgA + (size_t)bi * A_BAND, A_BAND / 2, &s.bar_a);
-        bulk_g2s(s.u.g.A + A_BAND / 2, imgA + (size_t)bi * A_BAND + A_BAND / 2, A_BAND / 2, &s.bar_a);
-        mbar_arrive_expect_tx(&s.bar_b, B_BAND);
-        bulk_g2s(s.u.g.B, imgB + (size_t)bj * B_BAND, B_BAND, &s.bar_b);
+        mbar_arrive_expect_tx(&s.bar_a, AB);
+        bulk_g2s(sA, imgA + (size_t)bi * AB, AB / 2, &s.bar_a);
+        bulk_g2s(sA + AB / 2, imgA + (size_t)bi * AB + AB / 2, AB / 2, &s.bar_a);
+        mbar_arrive_expect_tx(&s.bar_b, BB);
+        bulk_g2s(sB, imgB + (size_t)bj * BB, BB, &s.bar_b);
     }
     bool ok = true;
-    bool new_band = true;
+    bool new_band = true, first = true;
     const int q = warp & 3, hcol = warp >> 2;  // TMEM lane quadrant, column half of this warp
     const int rloc = 32 * q + lane;
     while (bi < nbi) {
         int nbi2 = bi, nbj2 = bj;
         next_tile(nbi2, nbj2);
-        // this thread's row and 16 columns of C, and their exponents, fetched before
+        // this thread's row and CW columns of C, and its row scale, fetched before
         // the MMAs complete so the memory latency hides behind the tensor core
         const int row = bi * MT_M + rloc;
         const bool row_ok = row < m;
-        const int ea_r = row_ok ? gea[row] : 0;
-        float4 cpre[16];
+        const float ea_r = row_ok ? gea[row] : 0.0f;
+        float4 cpre[CW];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const int col = bj * MT_N + 16 * hcol + j;
+        for (int j = 0; j < CW; ++j) {
+            const int col = bj * TN + CW * hcol + j;
             cpre[j] = (row_ok && col < nn) ? C[row + (size_t)col * ldc] : make_float4(0, 0, 0, 0);
         }
         if (tid == 0) {
             bool w = true;
             if (new_band) {
-                w = mbar_wait(&s.bar_a, ph.a);
+                w = mbar_wait(&s.bar_a, ph.a, first ? X.first_wait : WAIT_LIMIT);
+                if (!w) mbar_wait(&s.bar_a, ph.a);  // let the copy in flight land before moving on
                 ph.a ^= 1;
             }
-            w = w && mbar_wait(&s.bar_b, ph.b);
+            const bool wb = mbar_wait(&s.bar_b, ph.b);
             ph.b ^= 1;
-            if (!w) s.err = 1;
-            tc_fence_after();
-            issue_tile_mmas(s, tmem);
-        }
-        const bool mw = mbar_wait(&s.bar_mma, ph.mma);
-        ph.mma ^= 1;
-        if (!mw && lane == 0) s.err = 1;
-        if (tid == 0 && nbi2 < nbi) {  // operands of the next tile: smem is free once the MMAs completed
-            if (nbi2 != bi) {
-                mbar_arrive_expect_tx(&s.bar_a, A_BAND);
-                bulk_g2s(s.u.g.A, imgA + (size_t)nbi2 * A_BAND, A_BAND / 2, &s.bar_a);
-                bulk_g2s(s.u.g.A + A_BAND / 2, imgA + (size_t)nbi2 * A_BAND + A_BAND / 2, A_BAND / 2, &s.bar_a);
+            if (w && wb) {
+                tc_fence_after();
+                issue_tile_mmas<NS>(smem_u32(sA), smem_u32(sB), &s.bar_mma, tmem);
+            } else {
+                s.err = 1;                // operands missing: no MMA is issued, the CTA stops
+                mbar_arrive(&s.bar_mma);  // after this tile; release its MMA wait at once
             }
-            mbar_arrive_expect_tx(&s.bar_b, B_BAND);
-            bulk_g2s(s.u.g.B, imgB + (size_t)nbj2 * B_BAND, B_BAND, &s.bar_b);
+        }
+        first = false;
+        const bool mw = mbar_wait(&s.bar_mma, ph.mma);
+        if (!mw && lane == 0) {
+            s.err = 1;
+            s.mma_stuck = 1 + (int)ph.mma;
+        }
+        ph.mma ^= 1;
+        // operands of the next tile: smem is free once the MMAs completed (none after a failed wait)
+        if (tid == 0 && nbi2 < nbi && !s.err) {
+            if (nbi2 != bi) {
+                mbar_arrive_expect_tx(&s.bar_a, AB);
+                bulk_g2s(sA, imgA + (size_t)nbi2 * AB, AB / 2, &s.bar_a);
+                bulk_g2s(sA + AB / 2, imgA + (size_t)nbi2 * AB + AB / 2, AB / 2, &s.bar_a);
+            }
+            mbar_arrive_expect_tx(&s.bar_b, BB);
+            bulk_g2s(sB, imgB + (size_t)nbj2 * BB, BB, &s.bar_b);
         }
         tc_fence_after();
-        // epilogue: TMEM lanes 32(w%4).. (rows), columns 16(w/4)..+15
+        // epilogue: TMEM lanes 32(w%4).. (rows), columns CW(w/4)..+CW-1
 #pragma unroll
-        for (int cc = 0; cc < 16; cc += 4) {
-            float g[6][4];
-            const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + 16 * hcol + cc;
+        for (int cc = 0; cc < CW; cc += 4) {
+            float g[2 * NG][4];
+            const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + CW * hcol + cc;
 #pragma unroll
-            for (int a = 0; a < 6; ++a) tmem_ld4(base + 32 * a, g[a]);
+            for (int a = 0; a < 2 * NG; ++a) tmem_ld4(base + TN * a, g[a]);
             tmem_wait_ld();
             if (row_ok) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const int col = bj * MT_N + 16 * hcol + cc + j;
+                    const int col = bj * TN + CW * hcol + cc + j;
                     if (col < nn) {
-                        const float sc = ldexpf(1.0f, ea_r + __ldg(geb + col) - 16);
+                        const float sc = ea_r * __ldg(geb + col);  // 2^(ea+eb-16), exact
                         const float4 cv = cpre[cc + j];
                         dfc c = dfc{df{cv.x, cv.y}, df{cv.z, cv.w}};
-                        // c - (L0 + L1 + L23) sc: level 0 and level 1 enter exactly (integers
-                        // times a power of two, two-sums), level 2+3 and every error term in one
-                        // FP32 accumulator, one renormalisation per component
-                        c.re = df_sub_levels(c.re, g[0][j] * sc, g[2][j] * sc, g[4][j] * sc);
-                        c.im = df_sub_levels(c.im, g[1][j] * sc, g[3][j] * sc, g[5][j] * sc);
+                        float lr[NG], li[NG];
+#pragma unroll
+                        for (int gg = 0; gg < NG; ++gg) {
+                            lr[gg] = g[2 * gg][j] * sc;
+                            li[gg] = g[2 * gg + 1][j] * sc;
+                        }
+                        c.re = df_sub_levels<NG>(c.re, lr);
+                        c.im = df_sub_levels<NG>(c.im, li);
                         dfc_store(C + row + (size_t)col * ldc, c);
                     }
                 }
@@ -625,6 +686,7 @@ static __device__ void df_swaps_trsm(float4* __restrict__ A, int n, int j0, int 
     __syncthreads();
 }
 
+template <int NS>
 static __device__ bool lu_mixed(float4* __restrict__ A, int n, int* __restrict__ ipiv, MixSmem& s, const MixScratch& X,
                          uint32_t tmem, Phases& ph) {
     for (int j0 = 0; j0 < n; j0 += NB) {
@@ -635,7 +697,7 @@ static __device__ bool lu_mixed(float4* __restrict__ A, int n, int* __restrict__
         df_swaps_trsm(A, n, j0, jb, ipiv, s);
         stat_add(s, PH_TRSM);
         const int r0 = j0 + jb;
-        if (!mixed_gemm_sub(A + r0 + (size_t)r0 * n, n, A + r0 + (size_t)j0 * n, n, A + j0 + (size_t)r0 * n, n,
+        if (!mixed_gemm_sub<NS>(A + r0 + (size_t)r0 * n, n, A + r0 + (size_t)j0 * n, n, A + j0 + (size_t)r0 * n, n,
                             n - r0, n - r0, jb, 0, s, X, tmem, ph))
             return false;
     }
@@ -643,6 +705,7 @@ static __device__ bool lu_mixed(float4* __restrict__ A, int n, int* __restrict__
 }
 
 // tr(A^-1 B) from the mixed LU of A; B (double-float, n x n) is destroyed
+template <int NS>
 static __device__ bool trace_solve_mixed(const float4* __restrict__ A, float4* __restrict__ B, int n,
                                   const int* __restrict__ ipiv, MixSmem& s, const MixScratch& X, uint32_t tmem,
                                   Phases& ph, zc& out) {
@@ -661,7 +724,7 @@ static __device__ bool trace_solve_mixed(const float4* __restrict__ A, float4* _
         for (int col = tid; col < n; col += NT) dcol_lower_unit(B + (size_t)col * n + j0, jb, s.u.p.T);
         __syncthreads();
         const int r0 = j0 + jb;
-        if (!mixed_gemm_sub(B + r0, n, A + r0 + (size_t)j0 * n, n, B + j0, n, n - r0, n, jb, 0, s, X, tmem, ph))
+        if (!mixed_gemm_sub<NS>(B + r0, n, A + r0 + (size_t)j0 * n, n, B + j0, n, n - r0, n, jb, 0, s, X, tmem, ph))
             return false;
     }
     const int nblk = (n + NB - 1) / NB;
@@ -670,7 +733,7 @@ static __device__ bool trace_solve_mixed(const float4* __restrict__ A, float4* _
         load_upper_block(A, n, j0, jb, s);
         for (int col = tid; col < ncol; col += NT) dcol_upper(B + (size_t)col * n + j0, jb, s.u.p.T);
         __syncthreads();
-        if (!mixed_gemm_sub(B, n, A + (size_t)j0 * n, n, B + j0, n, j0, ncol, jb, 1, s, X, tmem, ph)) return false;
+        if (!mixed_gemm_sub<NS>(B, n, A + (size_t)j0 * n, n, B + j0, n, j0, ncol, jb, 1, s, X, tmem, ph)) return false;
     }
     double tr = 0.0, ti = 0.0, z = 0.0;
     for (int i = tid; i < n; i += NT) {
@@ -683,13 +746,19 @@ static __device__ bool trace_solve_mixed(const float4* __restrict__ A, float4* _
     return true;
 }
 
-// assembly in FP64, stored double-float; returns the largest |entry| seen
+// (largest, smallest non-zero) of max(|Re|, |Im|) over the entries seen, with v added
+__device__ __forceinline__ float2 entry_range(float2 rg, float4 v) {
+    const float a = fmaxf(fabsf(v.x), fabsf(v.z));
+    return make_float2(fmaxf(rg.x, a), a > 0.0f ? fminf(rg.y, a) : rg.y);
+}
+
 // One 32 x 32 tile of a d != 3 matrix (K_nu elements, FP64, grouped by regime)
 // stored as double-floats: the direct triangle here, the mirror by the caller.
 // Not inlined, so that d = 3 matrices keep the kernel's registers for themselves.
-static __device__ __noinline__ float assemble_tile_grouped(float4* __restrict__ A, float4* __restrict__ B, int n, int d,
-                                                   const double* __restrict__ pos, zc k, int I, int J, zc dg0,
-                                                   zc dg1, MixSmem& s, float mx) {
+// rg: the largest and the smallest non-zero max(|Re|, |Im|) of the entries seen.
+static __device__ __noinline__ float2 assemble_tile_grouped(float4* __restrict__ A, float4* __restrict__ B, int n,
+                                                    int d, const double* __restrict__ pos, zc k, int I, int J,
+                                                    zc dg0, zc dg1, MixSmem& s, float2 rg) {
     const int tid = threadIdx.x;
     auto cvt = [](zc v) {
         df a = df_from_double(v.re), b = df_from_double(v.im);
@@ -697,11 +766,11 @@ static __device__ __noinline__ float assemble_tile_grouped(float4* __restrict__ 
     };
     tile_pairs_grouped(I, J, n, d, pos, k, B != nullptr, s.u.p.list, s.u.p.cnt, [&](int ii, int jj, zc m, zc dm) {
         const float4 fm = cvt(m);
-        mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+        rg = entry_range(rg, fm);
         s.u.p.T[jj][ii] = fm;
         if (B) {
             const float4 fd = cvt(dm);
-            mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+            rg = entry_range(rg, fd);
             s.u.p.T2[jj][ii] = fd;
         }
     });
@@ -714,21 +783,94 @@ static __device__ __noinline__ float assemble_tile_grouped(float4* __restrict__ 
             if (B) fd = s.u.p.T2[jj][ii];
             if (i == j) {
                 fm = cvt(dg0);
-                mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                rg = entry_range(rg, fm);
                 if (B) {
                     fd = cvt(dg1);
-                    mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                    rg = entry_range(rg, fd);
                 }
             }
             A[i + (size_t)j * n] = fm;
             if (B) B[i + (size_t)j * n] = fd;
         }
     }
-    return mx;
+    return rg;
 }
 
+// One 32 x 32 tile of a d = 2 matrix, every element on the FP32 pipe in
+// double-float (green_df2.cuh), the pairs grouped by K_nu regime as in the
+// FP64 engine (tile_pairs_grouped): classified into three shared-memory lists,
+// then consecutive threads take consecutive list entries, so that a warp runs
+// one regime's loop.  Direct triangle here, the mirror by the caller.
+static __device__ __noinline__ float2 assemble_tile_grouped_df2(float4* __restrict__ A, float4* __restrict__ B, int n,
+                                                        int I, int J, zc dg0, zc dg1, MixSmem& s, float2 rg) {
+    const int tid = threadIdx.x;
+    const Df2Item& P = s.u.p.d2;
+    unsigned short* list = s.u.p.list;
+    int* cnt = s.u.p.cnt;
+    auto dist = [&](int ii, int jj) {
+        const float4 pa = s.u.p.ci[ii], pb = s.u.p.cj[jj];
+        const df ex = df_sub(df{pa.x, pa.y}, df{pb.x, pb.y});
+        const df ey = df_sub(df{pa.z, pa.w}, df{pb.z, pb.w});
+        return df_sqrt(df_add(df_mul(ex, ex), df_mul(ey, ey)));
+    };
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int p = tid + NT * q, ii = p & 31, jj = p >> 5;
+        const int i = I * 32 + ii, j = J * 32 + jj;
+        if (i < n && j < n && i < j) {
+            const int reg = k_regime_df(P, dist(ii, jj));
+            list[reg * 1024 + atomicAdd(&cnt[reg], 1)] = (unsigned short)p;
+        }
+    }
+    __syncthreads();
+    const int c0 = cnt[0], c1 = cnt[1], tot = c0 + c1 + cnt[2];
+    for (int w = tid; w < tot; w += NT) {
+        const int reg = w < c0 ? 0 : (w < c0 + c1 ? 1 : 2);
+        const int p = reg == 0 ? list[w] : (reg == 1 ? list[1024 + w - c0] : list[2048 + w - c0 - c1]);
+        const int ii = p & 31, jj = p >> 5;
+        dfc m, dm;
+        pair_elements_df2(s.u.p.tab, P, dist(ii, jj), reg, B != nullptr, m, dm);
+        const float4 fm = make_float4(m.re.h, m.re.l, m.im.h, m.im.l);
+        rg = entry_range(rg, fm);
+        s.u.p.T[jj][ii] = fm;
+        if (B) {
+            const float4 fd = make_float4(dm.re.h, dm.re.l, dm.im.h, dm.im.l);
+            rg = entry_range(rg, fd);
+            s.u.p.T2[jj][ii] = fd;
+        }
+    }
+    __syncthreads();
+    if (tid < 3) cnt[tid] = 0;
+    auto cvt = [](zc v) {
+        df a = df_from_double(v.re), b = df_from_double(v.im);
+        return make_float4(a.h, a.l, b.h, b.l);
+    };
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ii = tid & 31, jj = (tid >> 5) + 8 * q;
+        const int i = I * 32 + ii, j = J * 32 + jj;
+        if (i < n && j < n && i <= j) {
+            float4 fm = s.u.p.T[jj][ii], fd = make_float4(0, 0, 0, 0);
+            if (B) fd = s.u.p.T2[jj][ii];
+            if (i == j) {
+                fm = cvt(dg0);
+                rg = entry_range(rg, fm);
+                if (B) {
+                    fd = cvt(dg1);
+                    rg = entry_range(rg, fd);
+                }
+            }
+            A[i + (size_t)j * n] = fm;
+            if (B) B[i + (size_t)j * n] = fd;
+        }
+    }
+    return rg;
+}
+
+// Assembly of M(k) (and dM/dk into B) as double-floats; returns the largest
+// and the smallest non-zero max(|Re|, |Im|) over the entries this thread stored.
 template <bool D3ONLY>
-__device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int n, int d,
+__device__ float2 assemble_df(float4* __restrict__ A, float4* __restrict__ B, int n, int d,
                              const double* __restrict__ pos, const msgpu_model& mdl, zc k, MixSmem& s) {
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -741,10 +883,12 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
     const df kr = df_from_double(k.re), ki = df_from_double(k.im);
     const bool grow = k.im != 0.0;
     const bool grouped = !D3ONLY && d != 3 && d != 1;
-    if (d3) df3_tables_init(s.u.p.tab);
+    const bool d2 = !D3ONLY && d == 2;  // d = 2: every element on the FP32 pipe too (green_df2.cuh)
+    if (d3 || d2) df3_tables_init(s.u.p.tab);
+    if (d2 && tid == 0) s.u.p.d2 = df2_item(k);
     if (grouped && tid < 3) s.u.p.cnt[tid] = 0;
     __syncthreads();
-    float mx = 0.0f;
+    float2 rg = make_float2(0.0f, INFINITY);
     auto cvt = [](zc v) {
         df a = df_from_double(v.re), b = df_from_double(v.im);
         return make_float4(a.h, a.l, b.h, b.l);
@@ -752,15 +896,16 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
     const int nt = (n + 31) / 32;
     for (int J = 0; J < nt; ++J) {
         for (int I = 0; I <= J; ++I) {
-            if (d3) {
+            if (d3 || d2) {
                 // the tile's atoms as double-floats: rows I*32.., columns J*32..
                 if (tid < 64) {
                     const int a = (tid < 32 ? I : J) * 32 + (tid & 31);
+                    const int dd = d3 ? 3 : 2;
                     df x{0.0f, 0.0f}, y{0.0f, 0.0f}, z{0.0f, 0.0f};
                     if (a < n) {
-                        x = df_from_double(pos[3 * a]);
-                        y = df_from_double(pos[3 * a + 1]);
-                        z = df_from_double(pos[3 * a + 2]);
+                        x = df_from_double(pos[dd * a]);
+                        y = df_from_double(pos[dd * a + 1]);
+                        if (d3) z = df_from_double(pos[3 * a + 2]);
                     }
                     if (tid < 32) {
                         s.u.p.ci[tid] = make_float4(x.h, x.l, y.h, y.l);
@@ -773,7 +918,8 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                 __syncthreads();
             }
             if (grouped) {
-                mx = assemble_tile_grouped(A, B, n, d, pos, k, I, J, dg0, dg1, s, mx);
+                rg = d2 ? assemble_tile_grouped_df2(A, B, n, I, J, dg0, dg1, s, rg)
+                        : assemble_tile_grouped(A, B, n, d, pos, k, I, J, dg0, dg1, s, rg);
             } else {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -804,11 +950,11 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
                             fm = cvt(m);
                             if (B) fd = cvt(dm);
                         }
-                        mx = fmaxf(mx, fmaxf(fabsf(fm.x), fabsf(fm.z)));
+                        rg = entry_range(rg, fm);
                         A[i + (size_t)j * n] = fm;
                         s.u.p.T[jj][ii] = fm;
                         if (B) {
-                            mx = fmaxf(mx, fmaxf(fabsf(fd.x), fabsf(fd.z)));
+                            rg = entry_range(rg, fd);
                             B[i + (size_t)j * n] = fd;
                             s.u.p.T2[jj][ii] = fd;
                         }
@@ -828,7 +974,7 @@ __device__ float assemble_df(float4* __restrict__ A, float4* __restrict__ B, int
             __syncthreads();
         }
     }
-    return mx;
+    return rg;
 }
 
 // after block_argmax: the CTA-wide maximum (thread 0 folded the warp maxima into red_v)
@@ -1020,7 +1166,7 @@ template <int KIND, bool D3ONLY>
 __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScratch X)
 {
     extern __shared__ uint8_t smem_raw[];
-    MixSmem& s = *reinterpret_cast<MixSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    MixSmem& s = *reinterpret_cast<MixSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == 0) {
         tmem_alloc(&s.tmem, TMEM_COLS);
@@ -1031,6 +1177,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         mbar_init(&s.bar_b, 1);
         mbar_init(&s.bar_mma, 1);
         s.err = 0;
+        s.mma_stuck = 0;
         for (int i = 0; i < PH_N; ++i) s.stat[i] = 0;
         fence_mbar_init();
     }
@@ -1065,12 +1212,21 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         const MedDev md = P.media[P.item_med[it]];
         const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
         stat_start(s);
-        const float mx = assemble_df<D3ONLY>(A, B, md.n, md.d, md.pos, md.model, k, s);
+        const float2 rg = assemble_df<D3ONLY>(A, B, md.n, md.d, md.pos, md.model, k, s);
         stat_add(s, PH_ASSEMBLE);
         int dummy;
-        block_argmax((double)mx, tid, s, dummy);
+        block_argmax((double)rg.x, tid, s, dummy);
         const double mxd = block_max_value(s);
         __syncthreads();  // red_v is reused by the next reduction
+        block_argmax(-(double)rg.y, tid, s, dummy);
+        const double mnd = -block_max_value(s);
+        __syncthreads();
+        // six slices when the entries span more than SPAN_WIDE (or an entry is zero / non-finite),
+        // and for every dlogf item (near a root the condition number of M magnifies the LU's
+        // error in tr(M^-1 dM/dk)), if this launch has the shared memory for them; else four,
+        // and a status bit says so
+        const bool span_wide = KIND == 1 || !(mxd <= (double)SPAN_WIDE * mnd);
+        const bool wide = span_wide && P.wide_ok;
         zc res = mk(0.0);
         int st = 0;
         if (!(mxd < (double)RANGE_LIMIT)) {
@@ -1083,12 +1239,14 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
                 for (int i = tid; i < md.n; i += NT) vphi[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
                 __syncthreads();
             }
-            if (!lu_mixed(A, md.n, ipiv, s, X, tmem, ph)) {
+            if (!(wide ? lu_mixed<6>(A, md.n, ipiv, s, X, tmem, ph) : lu_mixed<4>(A, md.n, ipiv, s, X, tmem, ph))) {
                 alive = false;
             } else if (KIND == 0) {
                 res = tracelog_df(A, md.n, ipiv, s);
             } else if (KIND == 1) {
-                if (!trace_solve_mixed(A, B, md.n, ipiv, s, X, tmem, ph, res)) alive = false;
+                if (!(wide ? trace_solve_mixed<6>(A, B, md.n, ipiv, s, X, tmem, ph, res)
+                           : trace_solve_mixed<4>(A, B, md.n, ipiv, s, X, tmem, ph, res)))
+                    alive = false;
             } else {
                 res = refine_solve(A, Mc, vphi, vx, vr, vt, md, k, ipiv, s);
                 if (P.amps)
@@ -1104,6 +1262,7 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         }
         if (tid == 0) {
             s.stat[PH_ITEMS] += 1;
+            if (span_wide && !wide) st |= MSGPU_S_SPAN;
             P.out[2 * it] = res.re;
             P.out[2 * it + 1] = res.im;
             if (s.info) st |= MSGPU_S_SINGULAR;
@@ -1112,11 +1271,20 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         }
         __syncthreads();
     }
-    if (s.err && tid == 0) atomicExch(X.err, 1);
+    if (s.err && tid == 0) {
+        atomicExch(X.err, 1);
+        // the run is abandoned: every item not yet taken is marked, none keeps a stale result
+        for (unsigned q = atomicAdd(P.counter, 1u); q < P.counter[1] && (int)q < P.nitem;
+             q = atomicAdd(P.counter, 1u)) {
+            const int it = P.order[q];
+            P.out[2 * it] = P.out[2 * it + 1] = nan("");
+            P.status[it] = MSGPU_S_TIMEOUT;
+        }
+    }
     if (X.stats && tid == 0)
         for (int i = 0; i < PH_N; ++i) atomicAdd(X.stats + i, s.stat[i]);
-    // a timed-out wait may leave MMAs in flight: give them a bounded chance to land
-    if (s.err && tid == 0) mbar_wait(&s.bar_mma, ph.mma, 1 << 20);
+    // an MMA completion wait that ran out may leave MMAs in flight: give them a bounded chance to land
+    if (s.mma_stuck && tid == 0) mbar_wait(&s.bar_mma, (uint32_t)(s.mma_stuck - 1), 1 << 20);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);

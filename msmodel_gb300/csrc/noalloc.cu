@@ -121,6 +121,8 @@ extern "C" int msgpu_tracelog_batch_noalloc(int d, int n, const double* d_pos, m
     P.kind = 0;
     P.amps = nullptr;
     P.amp_off = nullptr;
+    P.wide_ok = 0;
+    P.warm = 0;
     k_engine_fp64<<<(unsigned)grid, NT, sizeof(LuSmem), st>>>(P);
     if (cudaGetLastError() != cudaSuccess) return record_error(MSGPU_E_CUDA, "noalloc: engine kernel launch failed");
     count_launches(2);

@@ -1,12 +1,13 @@
 // special.cu -- the device special-function kernel behind msgpu_eval_special
 // (engine.cu launches it): the Green functions, K_nu, F(k)^-1 and the mixed
-// engine's double-float d = 3 elements, evaluated point by point for the
+// engine's double-float d = 3 and d = 2 elements, evaluated point by point for the
 // checks against the reference goldens; a unit of its own so that it compiles
 // beside the engine.
 #include <cuda_runtime.h>
 #include "msgpu.h"
 #include "lu64.cuh"
 #include "green_df.cuh"
+#include "green_df2.cuh"
 #include "engine_internal.h"
 
 namespace msg {
@@ -42,6 +43,16 @@ __global__ void k_eval_special(int which, int d, msgpu_model m, int n, const dou
         pair_elements_df3t(tab, df_from_double(k.re), df_from_double(k.im), k.im != 0.0, df_from_double(r),
                            which == 8, a, b);
         const dfc e = which == 7 ? a : b;
+        v = mk(df_to_double(e.re), df_to_double(e.im));
+        break;
+    }
+    case 9:
+    case 10: {  // d = 2 matrix elements on the FP32 pipe, as the mixed engine assembles them
+        const Df2Item P = df2_item(k);
+        const df rd = df_from_double(r);
+        dfc a, b;
+        pair_elements_df2(tab, P, rd, k_regime_df(P, rd), which == 10, a, b);
+        const dfc e = which == 9 ? a : b;
         v = mk(df_to_double(e.re), df_to_double(e.im));
         break;
     }

@@ -56,10 +56,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
 
 // Bounded wait on an mbarrier phase: false after `limit` polls (the caller
 // records the timeout and unwinds; nothing spins forever).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int limit = 1 << 22) {
+constexpr int WAIT_LIMIT = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int limit = WAIT_LIMIT) {
     for (int i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
+}
+
+// plain arrival (count 1) on an mbarrier
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {

@@ -241,6 +241,7 @@ class Reference:
         L.ref_parse_cdata.argtypes = [C.c_int, C.c_char_p, _dp]
         L.ref_traceinv.argtypes = med + [C.c_int, _dp, _dp]
         L.ref_eigvals.argtypes = med + [_dp, _dp]
+        L.ref_chistogram.argtypes = [C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
         L.ref_inverse_iteration.argtypes = med + [_dp, _dp, _dp]
         L.ref_roots_muller.argtypes = [C.c_int] + med + [_dp, C.c_int, _dp, C.c_int, C.c_double]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
@@ -295,6 +296,15 @@ class Reference:
         mu = np.zeros(2 * n)
         self.L.ref_eigvals(*self._med(d, n, model, params, shape, ratio, seed), np.array([k.real, k.imag]), mu)
         return mu.view(np.complex128).copy()
+
+    def chistogram(self, mu, xbin, ybin, mbin):
+        """fill_chist of the complex values mu into a fresh xbin x ybin histogram with an
+        mbin marginal: (data[ybin, xbin], mdata[mbin], info dict)."""
+        z = _cplx_array(mu)
+        data, mdata, info = np.zeros(xbin * ybin), np.zeros(mbin), np.zeros(11)
+        self.L.ref_chistogram(len(z) // 2, z, xbin, ybin, mbin, data, mdata, info)
+        keys = ["xmin", "xmax", "ymin", "ymax", "mmin", "mmax", "avg_re", "avg_im", "sigma_re", "sigma_im", "lost"]
+        return data.reshape(ybin, xbin), mdata, dict(zip(keys, info.tolist()))
 
     def traceinv(self, d, n, seed, ks, model="maximum", params=(), shape="ball", ratio=1.0):
         kk = _cplx_array(ks)

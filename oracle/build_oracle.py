@@ -22,6 +22,8 @@ REF_SOURCES = [
     "ms_matrix_util.c", "green_bessel.c", "medium_util.c", "nru_random.c",
     "scattering_model_util.c", "real_vector_util.c", "complex_vector_util.c",
     "common_util.c", "root_finder.c", "domain_util.c", "complex_data_util.c",
+    # the mu-plane histogram binning (chistogram_util.c) and what its unit pulls in
+    "chistogram_util.c", "color_rule_util.c", "color_data_util.c", "tikz_util.c",
 ]
 
 

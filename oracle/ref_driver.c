@@ -20,6 +20,8 @@
 #include "complex_data_type.h"
 #include "complex_data_util.h"
 #include "scattering_model_util.h"
+#include "chistogram_type.h"
+#include "chistogram_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -277,4 +279,22 @@ void ref_eigvals(int d, int n, int mtype, int np, const double* p, int shape, do
     eigvals(n, a, (dcomplex*)mu);
     free(a);
     drop_medium(&med);
+}
+
+/* fill_chist (chistogram_util.c:253) of the nz complex values z into a fresh
+ * xbin x ybin histogram with an mbin marginal (init_chistogram, :31): data
+ * (row-major, top row = ymax), mdata, and info = {xmin, xmax, ymin, ymax, mmin,
+ * mmax, Re avg, Im avg, Re sigma, Im sigma, lost} */
+void ref_chistogram(int nz, const double* z, int xbin, int ybin, int mbin, double* data, double* mdata,
+                    double* info) {
+    Chistogram ch;
+    memset(&ch, 0, sizeof(ch));  /* domain and marginal range not set up: taken from the values */
+    init_chistogram(&ch, msmatrix, 0.0, 1, xbin, ybin, mbin, "");
+    const int lost = fill_chist(&ch, nz, (dcomplex*)z);
+    memcpy(data, ch.data, sizeof(double) * (size_t)xbin * ybin);
+    memcpy(mdata, ch.mdata, sizeof(double) * (size_t)mbin);
+    const double v[11] = {ch.dom->xmin, ch.dom->xmax, ch.dom->ymin, ch.dom->ymax, ch.mmin, ch.mmax,
+                          creal(ch.avgz), cimag(ch.avgz), creal(ch.sigmaz), cimag(ch.sigmaz), (double)lost};
+    memcpy(info, v, sizeof(v));
+    del_chistogram(&ch);
 }

@@ -14,7 +14,7 @@ time reads the reference).
    its sources into oracle/_ref, on the hot-path configurations at sizes that
    finish in seconds (seeded scatterers, ln det / N, dlogf, roots, psi).
 
-Usage:  [MSMODEL_REF=<reference tree>] python tests/golden/make_golden.py
+Usage:  [MSMODEL_REF=<reference tree>] python tests/golden/make_golden.py [--chistogram-only]
 """
 import ast
 import hashlib
@@ -165,6 +165,7 @@ def reference_runs():
     # eigenvalues of M(k) (eigvals, zgeev): the input of the mu-plane histograms
     for d, n, seed, k in ((3, 60, 1, 1.2 - 0.05j), (2, 50, 2, 0.8 + 0.0j)):
         add("eigvals", d=d, n=n, seed=seed, k=[k.real, k.imag], mu=_cl(r.eigvals(d, n, seed, k)))
+    runs["cases"].extend(chistogram_cases(r))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
@@ -172,7 +173,30 @@ def reference_runs():
     return runs
 
 
+def chistogram_cases(r):
+    """mu-plane histograms (run_chistogram_omp, ms_core.c:173-232): the
+    eigenvalues of M(k) of seeds 1..nseed binned by the reference's fill_chist."""
+    out = []
+    for d, n, nseed, k, xbin, ybin, mbin in ((3, 60, 3, 1.3, 16, 12, 10), (2, 50, 2, 2.0, 12, 9, 8)):
+        mus = [r.eigvals(d, n, s, k) for s in range(1, nseed + 1)]
+        data, mdata, info = r.chistogram(np.concatenate(mus), xbin, ybin, mbin)
+        out.append({"kind": "chistogram", "d": d, "n": n, "nseed": nseed, "k": [k, 0.0], "xbin": xbin,
+                    "ybin": ybin, "mbin": mbin, "mu": [_cl(m) for m in mus], "data": data.ravel().tolist(),
+                    "mdata": mdata.tolist(), "info": info})
+    return out
+
+
 if __name__ == "__main__":
+    if "--chistogram-only" in sys.argv:
+        # add or refresh only the mu-plane histogram cases of an existing reference_runs.json
+        from oracle import Reference
+        path = os.path.join(HERE, "reference_runs.json")
+        with open(path) as f:
+            runs = json.load(f)
+        runs["cases"] = [c for c in runs["cases"] if c["kind"] != "chistogram"] + chistogram_cases(Reference())
+        with open(path, "w") as f:
+            json.dump(runs, f, indent=0)
+        sys.exit(0)
     with open(os.path.join(HERE, "reference_tests.json"), "w") as f:
         json.dump(reference_tests(), f)
     with open(os.path.join(HERE, "reference_runs.json"), "w") as f:

@@ -23,3 +23,18 @@ def test_eigvals_reference_runs(ms, ref_runs):
             j = int(np.argmin([abs(m - w) for w in want]))
             assert abs(m - want[j]) < 1e-10 * scale
             want.pop(j)
+
+
+def test_run_chistogram_matches_reference(ms, ref_runs):
+    """run_chistogram_omp end to end: the eigenvalues of M(k) of seeds 1..nseed
+    on the GPU, binned as the reference bins its own (zgeev) eigenvalues.  The
+    eigen-solvers round differently (~1e-13), so a value on a bin edge may move:
+    at most two counts differ, the moments agree to 1e-10."""
+    for c in [c for c in ref_runs["cases"] if c["kind"] == "chistogram"]:
+        media = [ms.Medium(c["d"], c["n"], seed=s) for s in range(1, c["nseed"] + 1)]
+        h = ms.run_chistogram(media, complex(*c["k"]), c["xbin"], c["ybin"], c["mbin"])
+        assert np.all(h["status"] == 0)
+        assert np.abs(h["data"].ravel() - np.asarray(c["data"])).sum() <= 2
+        info = c["info"]
+        assert abs(h["avg"] - complex(info["avg_re"], info["avg_im"])) < 1e-10
+        assert abs(h["sigma"] - complex(info["sigma_re"], info["sigma_im"])) < 1e-10
