@@ -450,8 +450,10 @@ int msgpu_tracelog_matrix(int n, const double* mat, double* out, int* info) {
 // pair distances [rmin, rmax], on the diagonal |k| / (4 pi) and 1 / (4 pi).
 // The predicted span of the moduli, times 2 sqrt 2 (the engine measures
 // max(|Re|, |Im|), within sqrt 2 of the modulus), is compared with the
-// engine's threshold; anything not covered counts as wide.
+// engine's threshold for the job kind; anything not covered counts as wide.
 static bool item_may_be_wide(double rmin, double rmax, int kind, double kre, double kim) {
+    // the engine's thresholds: 2^8, or 2^20 for amplitude items (refined to an FP64 residual)
+    const double thr = kind == 2 ? 1048576.0 : 256.0;
     if (!(rmin > 0.0) || !(rmax >= rmin)) return true;
     const double a = -kim;
     auto g = [&](double r) { return std::exp(a * r) / r; };  // 4 pi |G|, up to the common factor
@@ -465,7 +467,7 @@ static bool item_may_be_wide(double rmin, double rmax, int kind, double kre, dou
         hi = std::max({hi, e1, e2, 1.0});
         lo = std::min({lo, e1, e2, 1.0});
     }
-    return !(hi <= lo * (256.0 / (2.0 * std::sqrt(2.0))));
+    return !(hi <= lo * (thr / (2.0 * std::sqrt(2.0))));
 }
 
 // Items of a job: medium of each, k, the queue order (largest matrices

@@ -53,6 +53,9 @@ constexpr int A_SUB = MT_M * NB * 2;    // one 128 x 32 bf16 operand tile: 8 KB
 constexpr int TMEM_COLS = 256;          // accumulators: 2 NG TN <= 192 columns (allocation rounded to 2^k)
 constexpr float RANGE_LIMIT = 1.0e18f;  // larger entries leave the safe FP32 exponent range
 constexpr float SPAN_WIDE = 256.0f;     // entry span above which an item is sliced six ways
+// amplitude items (iterative refinement to an FP64 residual): the LU only has to
+// make the refinement contract, so four slices serve up to a far larger span
+constexpr float SPAN_WIDE_REFINED = 1048576.0f;
 
 // slice configurations: NS slices per operand, TN tile columns, NG TMEM accumulator groups
 template <int NS> struct SliceCfg;
@@ -1221,11 +1224,12 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
         block_argmax(-(double)rg.y, tid, s, dummy);
         const double mnd = -block_max_value(s);
         __syncthreads();
-        // six slices when the entries span more than SPAN_WIDE (or an entry is zero / non-finite),
-        // and for every dlogf item (near a root the condition number of M magnifies the LU's
+        // six slices when the entries span more than SPAN_WIDE (SPAN_WIDE_REFINED for amplitude
+        // items) or an entry is zero / non-finite, and for every dlogf item (near a root the condition number of M magnifies the LU's
         // error in tr(M^-1 dM/dk)), if this launch has the shared memory for them; else four,
         // and a status bit says so
-        const bool span_wide = KIND == 1 || !(mxd <= (double)SPAN_WIDE * mnd);
+        const double thr = KIND == 2 ? (double)SPAN_WIDE_REFINED : (double)SPAN_WIDE;
+        const bool span_wide = KIND == 1 || !(mxd <= thr * mnd);
         const bool wide = span_wide && P.wide_ok;
         zc res = mk(0.0);
         int st = 0;
