@@ -182,7 +182,7 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
     // FP64 sweeps of a parked root count against the sweeps it has used, and
     // a root still in progress when its budget is spent fails.  The
     // Newton/Aberth update is FP64 throughout.
-    constexpr double SWITCH = 1e-7;
+    constexpr double SWITCH = 1e-9;
     // One sweep over every realisation: batched dlogf of the roots in progress
     // (flag 0) at precision prec, then the reference's sequential update.
     // Returns false when no root is in progress or on a GPU error.

@@ -38,7 +38,7 @@ def test_roots_match_oracle_batch(ms, oracle):
 
 def test_mixed_precision_roots(ms, ref_runs):
     """Mixed-precision dlogf far from the roots, FP64 dlogf from a relative
-    step of 1e-7 on, within the reference's budget of maxit sweeps per root:
+    step of 1e-9 on, within the reference's budget of maxit sweeps per root:
     the reference's root lists within 1e-8 |k|, none missing, none extra."""
     for c in [c for c in ref_runs["cases"] if c["kind"] == "aberth"]:
         med = ms.Medium(c["d"], c["n"], seed=c["seed"])
