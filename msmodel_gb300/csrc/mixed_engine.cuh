@@ -104,7 +104,6 @@ struct MixSmem {
     double red_v[NT / 32];
     int red_i[NT / 32];
     float red_f[NT / 32];
-    float4 rcp;  // reciprocal of the current pivot (double-float complex)
     double red_s[3][NT / 32];
     int info, bcast_i, item;
     unsigned long long stat[PH_N];
@@ -475,6 +474,16 @@ __device__ __forceinline__ int block_argmaxf(float v, int i, MixSmem& s) {
     return s.bcast_i;
 }
 
+// 1 / b in double-float, with b scaled by a power of two first so that its
+// squared modulus stays inside the FP32 range whatever the pivot's size
+__device__ __forceinline__ dfc dfc_recip_pow2(dfc b) {
+    int e;
+    frexpf(fmaxf(fabsf(b.re.h), fabsf(b.im.h)), &e);
+    const float sc = ldexpf(1.0f, -e);
+    const dfc r = dfc_recip(dfc{df{b.re.h * sc, b.re.l * sc}, df{b.im.h * sc, b.im.l * sc}});
+    return dfc{df{r.re.h * sc, r.re.l * sc}, df{r.im.h * sc, r.im.l * sc}};
+}
+
 // Panel factorisation in double-float: LAPACK's getf2 pivoting (|Re|+|Im|,
 // first index on ties, full-panel row interchanges), organised in sub-panels
 // of SW columns.  Inside a sub-panel the rank-1 updates touch only its own
@@ -483,6 +492,9 @@ __device__ __forceinline__ int block_argmaxf(float v, int i, MixSmem& s) {
 // matrix does not stay in L2 across 304 resident CTAs, so this cuts its
 // memory traffic (the full-width rank-1 form re-reads and re-writes the whole
 // remaining panel once per column) by about 2.4x at the same arithmetic.
+// The pivot's reciprocal is a double-float one that every thread computes
+// (the FP64 division by one thread, on a pipe at 1/64 of the FP32 rate, held
+// the whole CTA at the next barrier).
 // Not inlined: its registers are then allocated apart from the engine's
 // tensor-core epilogue, which holds the kernel at the 128-register cap.
 constexpr int SW = 4;
@@ -506,12 +518,8 @@ static __device__ __noinline__ void df_panel(float4* __restrict__ A, int n, int 
             if (tid == 0) {
                 ipiv[c] = p;
                 if (!nz && s.info == 0) s.info = c + 1;
-                if (nz) {  // the pivot's reciprocal, once per column, in FP64
-                    const zc rz = 1.0 / mk(df_to_double(piv.re), df_to_double(piv.im));
-                    const df a = df_from_double(rz.re), b = df_from_double(rz.im);
-                    s.rcp = make_float4(a.h, a.l, b.h, b.l);
-                }
             }
+            const dfc r = nz ? dfc_recip_pow2(piv) : dfc{df{0, 0}, df{0, 0}};
             __syncthreads();  // every thread holds the pivot before row p is swapped away
             if (nz && p != c && tid < jb) {
                 const size_t col = (size_t)(j0 + tid) * n;
@@ -525,7 +533,6 @@ static __device__ __noinline__ void df_panel(float4* __restrict__ A, int n, int 
             bv = -1.0f;
             bi = n;
             if (nz) {
-                const dfc r = dfc_load(&s.rcp);
                 for (int i = c + 1 + tid; i < n; i += NT) {
                     float4* pc = A + i + (size_t)c * n;
                     const dfc l = dfc_mul(dfc_load(pc), r);
@@ -675,9 +682,13 @@ static __device__ void load_upper_block(const float4* A, int n, int j0, int jb, 
     __syncthreads();
 }
 
-static __device__ void df_swaps_trsm(float4* __restrict__ A, int n, int j0, int jb, const int* __restrict__ ipiv, MixSmem& s) {
+// The panel's row interchanges on the columns outside it, then the TRSM
+// U12 = L11^-1 A12 of the columns right of it.  keep_l = false leaves the columns
+// left of the panel alone: a ln det reads only U's diagonal and the pivots.
+static __device__ void df_swaps_trsm(float4* __restrict__ A, int n, int j0, int jb, const int* __restrict__ ipiv,
+                                     MixSmem& s, bool keep_l) {
     load_lower_block(A, n, j0, jb, s);
-    for (int col = threadIdx.x; col < n; col += NT) {
+    for (int col = keep_l ? threadIdx.x : j0 + threadIdx.x; col < n; col += NT) {
         if (col >= j0 && col < j0 + jb) continue;
         float4* a = A + (size_t)col * n;
         for (int c = j0; c < j0 + jb; ++c) {
@@ -690,14 +701,14 @@ static __device__ void df_swaps_trsm(float4* __restrict__ A, int n, int j0, int 
 }
 
 template <int NS>
-static __device__ bool lu_mixed(float4* __restrict__ A, int n, int* __restrict__ ipiv, MixSmem& s, const MixScratch& X,
-                         uint32_t tmem, Phases& ph) {
+static __device__ bool lu_mixed(float4* __restrict__ A, int n, int* __restrict__ ipiv, bool keep_l, MixSmem& s,
+                                const MixScratch& X, uint32_t tmem, Phases& ph) {
     for (int j0 = 0; j0 < n; j0 += NB) {
         const int jb = min(NB, n - j0);
         stat_start(s);
         df_panel(A, n, j0, jb, ipiv, s);
         stat_add(s, PH_PANEL);
-        df_swaps_trsm(A, n, j0, jb, ipiv, s);
+        df_swaps_trsm(A, n, j0, jb, ipiv, s, keep_l);
         stat_add(s, PH_TRSM);
         const int r0 = j0 + jb;
         if (!mixed_gemm_sub<NS>(A + r0 + (size_t)r0 * n, n, A + r0 + (size_t)j0 * n, n, A + j0 + (size_t)r0 * n, n,
@@ -1243,7 +1254,8 @@ __global__ void __launch_bounds__(NT, 2) k_engine_mixed(EngineParams P, MixScrat
                 for (int i = tid; i < md.n; i += NT) vphi[i] = zexp(mk(0.0, 1.0) * k * md.pos[i * md.d]);
                 __syncthreads();
             }
-            if (!(wide ? lu_mixed<6>(A, md.n, ipiv, s, X, tmem, ph) : lu_mixed<4>(A, md.n, ipiv, s, X, tmem, ph))) {
+            if (!(wide ? lu_mixed<6>(A, md.n, ipiv, KIND != 0, s, X, tmem, ph)
+                       : lu_mixed<4>(A, md.n, ipiv, KIND != 0, s, X, tmem, ph))) {
                 alive = false;
             } else if (KIND == 0) {
                 res = tracelog_df(A, md.n, ipiv, s);
