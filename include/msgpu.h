@@ -236,10 +236,14 @@ int msgpu_find_roots_muller_batch(int method, int nmed, const msgpu_medium* medi
                                   int* nroots, int* nevals);
 
 /* The eigenvalues mu of M(k) per item (eigvals, src/core/ms_matrix_util.c:147,
- * the input of the mu-plane histograms, ms_core.c:173-282): M(k) assembled on
- * the GPU, the general complex eigenproblem solved by cuSOLVER (Xgeev, no
- * eigenvectors).  mu receives n complex values per item, items in order;
- * status (may be NULL) MSGPU_S_NOCONV where the QR iteration did not converge. */
+ * zgeev_ without eigenvectors; the input of the mu-plane histograms,
+ * ms_core.c:173-282), one kernel over the batch: each CTA assembles M(k),
+ * reduces it to Hessenberg form by Householder reflectors and takes its
+ * eigenvalues by single-shift complex QR (LAPACK's zgehd2 and zlahqr
+ * schemes, FP64, no balancing).  n <= 4097.  mu receives n complex values per
+ * item, items in order, in deflation order within an item; status (may be
+ * NULL) MSGPU_S_NOCONV where the QR iteration did not converge within
+ * 30 max(10, n) iterations (those values read 0). */
 int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
                         double* mu, int* status);
 

@@ -76,8 +76,7 @@ def build(force=False, verbose=False):
                 if verbose:
                     print("built", out)
     if force or jobs or _stale(LIB, objs):
-        # cuSOLVER: the general eigenproblem behind msgpu_eigvals_batch (not the hot path)
-        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcusolver", "-lm"]
+        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"]
         _compile((cmd, LIB))
     return LIB
 

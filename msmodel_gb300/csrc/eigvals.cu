@@ -1,12 +1,30 @@
 // eigvals.cu -- the eigenvalues mu of M(k), the input of the reference's
 // mu-plane histograms (eigvals, src/core/ms_matrix_util.c:147, zgeev_ without
 // eigenvectors; run_chistogram_omp and run_imag_mu_histogram_omp,
-// src/core/ms_core.c:173-282).  This is not the hot path: M(k) is assembled
-// on the GPU by this library's kernel, and the general complex eigenproblem
-// (Hessenberg reduction and shifted QR) is handed to cuSOLVER's Xgeev, one
-// matrix after another on one stream.
+// src/core/ms_core.c:173-282).
+//
+// One persistent CTA per matrix slot, FP64 throughout (the reference's
+// arithmetic), items dealt to CTAs in order:
+//   1. M(k) assembled by the FP64 engine's assembly (lu64.cuh);
+//   2. reduction to upper Hessenberg form by Householder reflectors, as
+//      LAPACK's unblocked zgehd2 (reflector of zlarfg; H applied from the
+//      right to rows 0..n-1, H^H from the left to the trailing rows), the
+//      reflector in shared memory, the right update one thread per row and the
+//      left update one warp per column (coalesced both ways);
+//   3. eigenvalues of the Hessenberg matrix by the single-shift complex QR
+//      algorithm of LAPACK's zlahqr with wantt = wantz = false (real
+//      subdiagonals, the Ahues-Kressner deflation test, Wilkinson shifts with
+//      exceptional shifts every 10 iterations without deflation, the search
+//      for two consecutive small subdiagonals, 2 x 2 reflectors chasing the
+//      bulge through the active block), run by the CTA's first warp: each
+//      bulge step is a chain of scalar work, and its row and column updates
+//      are split over the 32 lanes.
+// zgeev also balances the matrix first (zgebal); this path does not: M(k)'s
+// entries do not span the magnitudes balancing is for, and the eigenvalues
+// agree with the reference's to ~1e-13 of the largest.  Eigenvalues come out
+// in deflation order, as zgeev's.
 #include <cuda_runtime.h>
-#include <cusolverDn.h>
+#include <float.h>
 #include <algorithm>
 #include <mutex>
 #include <vector>
@@ -15,102 +33,386 @@
 #include "engine_internal.h"
 
 namespace msg {
-__global__ void __launch_bounds__(NT, 1) k_build_matrix(zc* A, int n, int d, const double* pos, msgpu_model m,
-                                                        double kre, double kim, int deriv);
+
+// shared memory: the assembly's and the reductions' LuSmem; the Householder
+// vector overlays its two tile buffers (4096 complex values: n <= 4097)
+constexpr int EIG_NMAX = NB * (TM + TN) + 1;
+
+struct EigParams {
+    int nitem;
+    const int* item_n;       // order per item
+    const int* item_d;
+    const size_t* item_pos;  // offset of the item's positions in pos
+    const msgpu_model* item_model;
+    const double* pos;
+    const double* ks;        // 2 per item
+    const size_t* item_out;  // offset of the item's eigenvalues in mu
+    zc* mu;
+    int* status;
+    zc* work;                // one nmax x nmax slot per CTA
+    size_t slot;
+};
+
+__device__ __forceinline__ double dlapy3(double x, double y, double z) {
+    const double w = fmax(fabs(x), fmax(fabs(y), fabs(z)));
+    if (w == 0.0) return fabs(x) + fabs(y) + fabs(z);
+    const double a = x / w, b = y / w, c = z / w;
+    return w * sqrt(a * a + b * b + c * c);
+}
+
+// Householder reduction to upper Hessenberg form (zgehd2, ilo = 1, ihi = n)
+static __device__ void hessenberg(zc* __restrict__ A, int n, LuSmem& s) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    zc* v = &s.As[0][0];
+    for (int j = 0; j + 2 < n; ++j) {
+        const int m = n - j - 1;  // length of the reflector
+        zc* col = A + (size_t)j * n + j + 1;
+        double ss = 0.0, z1 = 0.0, z2 = 0.0;
+        for (int i = 1 + tid; i < m; i += NT) ss += zabs2(col[i]);
+        block_sum3(ss, z1, z2, s);
+        const zc alpha = col[0];
+        __syncthreads();  // every thread has read alpha before column j changes
+        if (ss == 0.0 && alpha.im == 0.0) continue;  // H = I (tau = 0)
+        // zlarfg: beta = -sign(Re alpha) |(alpha, x)|, tau = (beta - alpha) / beta,
+        // v = (1, x / (alpha - beta))
+        const double beta = -copysign(dlapy3(alpha.re, alpha.im, sqrt(ss)), alpha.re);
+        const zc tau = mk((beta - alpha.re) / beta, -alpha.im / beta);
+        const zc scal = 1.0 / (alpha - beta);
+        for (int i = tid; i < m; i += NT) {
+            v[i] = i == 0 ? mk(1.0) : col[i] * scal;
+            col[i] = i == 0 ? mk(beta) : mk(0.0);
+        }
+        __syncthreads();
+        // from the right: A[0:n, j+1:n] -= tau (A v) v^H
+        for (int r = tid; r < n; r += NT) {
+            zc* row = A + r + (size_t)(j + 1) * n;
+            zc w = mk(0.0);
+            for (int c = 0; c < m; ++c) w += row[(size_t)c * n] * v[c];
+            w = tau * w;
+            for (int c = 0; c < m; ++c) row[(size_t)c * n] -= w * conjz(v[c]);
+        }
+        __syncthreads();
+        // from the left with conj(tau): A[j+1:n, j+1:n] -= conj(tau) v (v^H A)
+        const zc ctau = conjz(tau);
+        for (int c = j + 1 + warp; c < n; c += NT / 32) {
+            zc* cc = A + (size_t)c * n + j + 1;
+            zc w = mk(0.0);
+            for (int i = lane; i < m; i += 32) w += conjz(v[i]) * cc[i];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                w.re += __shfl_xor_sync(0xffffffffu, w.re, off);
+                w.im += __shfl_xor_sync(0xffffffffu, w.im, off);
+            }
+            w = ctau * w;
+            for (int i = lane; i < m; i += 32) cc[i] -= v[i] * w;
+        }
+        __syncthreads();
+    }
+}
+
+// zlarfg for n = 2: on return a = beta (real), x scaled, the reflector
+// I - tau (1, x)(1, x)^H
+__device__ __forceinline__ zc larfg2(zc& a, zc& x) {
+    const double xnorm = zabs(x);
+    if (xnorm == 0.0 && a.im == 0.0) return mk(0.0);
+    const double beta = -copysign(dlapy3(a.re, a.im, xnorm), a.re);
+    const zc tau = mk((beta - a.re) / beta, -a.im / beta);
+    x = x * (1.0 / (a - beta));
+    a = mk(beta);
+    return tau;
+}
+
+// Eigenvalues of the upper Hessenberg H (n x n, ld n) into w by zlahqr's
+// single-shift QR (wantt = wantz = false); run by one warp, every lane taking
+// the same scalar path.  Returns 0, or i + 1 if eigenvalue i and above did not
+// converge within 30 max(10, n) iterations (zlahqr's info).
+static __device__ int hqr_warp(zc* __restrict__ H, int n, zc* __restrict__ w) {
+    const int lane = threadIdx.x & 31;
+    auto h = [&](int r, int c) -> zc& { return H[r + (size_t)c * n]; };
+    if (n == 1) {
+        if (lane == 0) w[0] = h(0, 0);
+        return 0;
+    }
+    const int ilo = 0, ihi = n - 1;
+    // subdiagonal entries made real by diagonal unitary similarity
+    for (int i = ilo + 1; i <= ihi; ++i) {
+        const zc hs = h(i, i - 1);
+        __syncwarp();
+        if (hs.im != 0.0) {
+            zc sc = hs / abs1(hs);
+            sc = conjz(sc) / zabs(sc);
+            if (lane == 0) h(i, i - 1) = mk(zabs(hs));
+            for (int j = i + lane; j <= ihi; j += 32) h(i, j) = h(i, j) * sc;
+            __syncwarp();
+            const int top = min(ihi, i + 1);
+            for (int j = ilo + lane; j <= top; j += 32) h(j, i) = h(j, i) * conjz(sc);
+        }
+        __syncwarp();
+    }
+    const double safmin = DBL_MIN, ulp = DBL_EPSILON;
+    const double smlnum = safmin * ((double)(ihi - ilo + 1) / ulp);
+    const int itmax = 30 * max(10, ihi - ilo + 1);
+    constexpr int KEXSH = 10;
+    int kdefl = 0;
+    int i = ihi;
+    while (i >= ilo) {
+        int l = ilo;
+        bool done = false;
+        for (int its = 0; its <= itmax; ++its) {
+            // a single small subdiagonal element
+            int k;
+            for (k = i; k > l; --k) {
+                const zc hkk1 = h(k, k - 1);
+                if (abs1(hkk1) <= smlnum) break;
+                double tst = abs1(h(k - 1, k - 1)) + abs1(h(k, k));
+                if (tst == 0.0) {
+                    if (k - 2 >= ilo) tst += fabs(h(k - 1, k - 2).re);
+                    if (k + 1 <= ihi) tst += fabs(h(k + 1, k).re);
+                }
+                if (fabs(hkk1.re) <= ulp * tst) {
+                    const double a1 = abs1(hkk1), a2 = abs1(h(k - 1, k));
+                    const double ab = fmax(a1, a2), ba = fmin(a1, a2);
+                    const double b1 = abs1(h(k, k)), b2 = abs1(h(k - 1, k - 1) - h(k, k));
+                    const double aa = fmax(b1, b2), bb = fmin(b1, b2);
+                    const double sab = aa + ab;
+                    if (ba * (ab / sab) <= fmax(smlnum, ulp * (bb * (aa / sab)))) break;
+                }
+            }
+            l = k;
+            __syncwarp();
+            if (l > ilo && lane == 0) h(l, l - 1) = mk(0.0);
+            __syncwarp();
+            if (l >= i) {
+                done = true;
+                break;
+            }
+            ++kdefl;
+            const int i1 = l, i2 = i;  // the active block
+            zc t;
+            if (kdefl % (2 * KEXSH) == 0) {
+                t = h(i, i) + 0.75 * fabs(h(i, i - 1).re);
+            } else if (kdefl % KEXSH == 0) {
+                t = h(l, l) + 0.75 * fabs(h(l + 1, l).re);
+            } else {  // Wilkinson's shift
+                t = h(i, i);
+                const zc u = zsqrt(h(i - 1, i)) * zsqrt(h(i, i - 1));
+                double s = abs1(u);
+                if (s != 0.0) {
+                    const zc x = 0.5 * (h(i - 1, i - 1) - t);
+                    const double sx = abs1(x);
+                    s = fmax(s, sx);
+                    const zc xs = x / s, us = u / s;
+                    zc y = s * zsqrt(xs * xs + us * us);
+                    if (sx > 0.0) {
+                        const zc xn = x / sx;
+                        if (xn.re * y.re + xn.im * y.im < 0.0) y = -y;
+                    }
+                    t = t - u * (u / (x + y));
+                }
+            }
+            // two consecutive small subdiagonal elements: start the sweep at row m
+            int m;
+            zc v0, v1;
+            for (m = i - 1; m > l; --m) {
+                const zc h11 = h(m, m), h22 = h(m + 1, m + 1);
+                zc h11s = h11 - t;
+                double h21 = h(m + 1, m).re;
+                const double s = abs1(h11s) + fabs(h21);
+                h11s = h11s / s;
+                h21 /= s;
+                v0 = h11s;
+                v1 = mk(h21);
+                const double h10 = h(m, m - 1).re;
+                if (fabs(h10) * fabs(h21) <= ulp * (abs1(h11s) * (abs1(h11) + abs1(h22)))) break;
+            }
+            if (m == l) {
+                const zc h11 = h(l, l);
+                zc h11s = h11 - t;
+                double h21 = h(l + 1, l).re;
+                const double s = abs1(h11s) + fabs(h21);
+                v0 = h11s / s;
+                v1 = mk(h21 / s);
+            }
+            // the single-shift QR sweep
+            for (int kk = m; kk < i; ++kk) {
+                if (kk > m) {
+                    v0 = h(kk, kk - 1);
+                    v1 = h(kk + 1, kk - 1);
+                }
+                const zc t1 = larfg2(v0, v1);
+                __syncwarp();
+                if (kk > m && lane == 0) {
+                    h(kk, kk - 1) = v0;
+                    h(kk + 1, kk - 1) = mk(0.0);
+                }
+                const zc v2 = v1;
+                const double t2 = (t1 * v2).re;
+                // from the left: rows kk, kk+1, columns kk..i2
+                const zc ct1 = conjz(t1);
+                for (int j = kk + lane; j <= i2; j += 32) {
+                    const zc sum = ct1 * h(kk, j) + t2 * h(kk + 1, j);
+                    h(kk, j) -= sum;
+                    h(kk + 1, j) -= sum * v2;
+                }
+                __syncwarp();
+                // from the right: columns kk, kk+1, rows i1..min(kk+2, i)
+                const zc cv2 = conjz(v2);
+                const int jt = min(kk + 2, i);
+                for (int j = i1 + lane; j <= jt; j += 32) {
+                    const zc sum = t1 * h(j, kk) + t2 * h(j, kk + 1);
+                    h(j, kk) -= sum;
+                    h(j, kk + 1) -= sum * cv2;
+                }
+                __syncwarp();
+                if (kk == m && m > l) {
+                    // the sweep started below l: keep H(m, m-1) real
+                    zc temp = 1.0 - t1;
+                    temp = temp / zabs(temp);
+                    if (lane == 0) {
+                        h(m + 1, m) = h(m + 1, m) * conjz(temp);
+                        if (m + 2 <= i) h(m + 2, m + 1) = h(m + 2, m + 1) * temp;
+                    }
+                    __syncwarp();
+                    for (int j = m; j <= i; ++j) {
+                        if (j == m + 1) continue;
+                        for (int c = j + 1 + lane; c <= i2; c += 32) h(j, c) = h(j, c) * temp;
+                        for (int r = i1 + lane; r < j; r += 32) h(r, j) = h(r, j) * conjz(temp);
+                        __syncwarp();
+                    }
+                }
+            }
+            // H(i, i-1) made real
+            const zc temp = h(i, i - 1);
+            __syncwarp();
+            if (temp.im != 0.0) {
+                const double rt = zabs(temp);
+                const zc u = temp / rt;
+                if (lane == 0) h(i, i - 1) = mk(rt);
+                for (int c = i + 1 + lane; c <= i2; c += 32) h(i, c) = h(i, c) * conjz(u);
+                for (int r = i1 + lane; r < i; r += 32) h(r, i) = h(r, i) * u;
+            }
+            __syncwarp();
+        }
+        if (!done) return i + 1;
+        if (lane == 0) w[i] = h(i, i);
+        __syncwarp();
+        kdefl = 0;
+        i = l - 1;
+    }
+    return 0;
+}
+
+__global__ void __launch_bounds__(NT, 2) k_eigvals(EigParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LuSmem& s = *reinterpret_cast<LuSmem*>(smem_raw);
+    zc* A = P.work + (size_t)blockIdx.x * P.slot;
+    for (int it = blockIdx.x; it < P.nitem; it += gridDim.x) {
+        const int n = P.item_n[it];
+        const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
+        assemble(A, nullptr, n, P.item_d[it], P.pos + P.item_pos[it], P.item_model[it], k, s);
+        __syncthreads();
+        hessenberg(A, n, s);
+        int info = 0;
+        if (threadIdx.x < 32) info = hqr_warp(A, n, P.mu + P.item_out[it]);
+        if (threadIdx.x == 0) P.status[it] = info > 0 ? MSGPU_S_NOCONV : 0;
+        __syncthreads();
+    }
+}
+
 }  // namespace msg
 
 namespace {
 std::mutex g_eig_mu;
-cusolverDnHandle_t g_solver = nullptr;
-cusolverDnParams_t g_params = nullptr;
-}  // namespace
+}
 
 extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med,
                                    const double* ks, double* mu, int* status) {
     using namespace msg;
     if (nmed < 1 || !media || nitem < 1 || !ks || !mu) return MSGPU_E_ARG;
     int nmax = 0;
+    size_t npos = 0;
+    std::vector<size_t> med_pos(nmed);
     for (int m = 0; m < nmed; ++m) {
         if (media[m].n < 1 || media[m].d < 1 || !media[m].pos) return MSGPU_E_ARG;
         nmax = std::max(nmax, media[m].n);
+        med_pos[m] = npos;
+        npos += (size_t)media[m].n * media[m].d;
     }
+    if (nmax > EIG_NMAX) return MSGPU_E_SIZE;
     for (int i = 0; i < nitem; ++i)
         if (item_med && (item_med[i] < 0 || item_med[i] >= nmed)) return MSGPU_E_ARG;
     const int sms = msgpu_sm_count();  // initialises the device and the kernels' attributes
     if (sms < 1) return MSGPU_E_NODEV;
     std::lock_guard<std::mutex> lk(g_eig_mu);
-    if (!g_solver && (cusolverDnCreate(&g_solver) != CUSOLVER_STATUS_SUCCESS ||
-                      cusolverDnCreateParams(&g_params) != CUSOLVER_STATUS_SUCCESS))
-        return MSGPU_E_CUDA;
-    double* dpos = nullptr;
-    zc *dA = nullptr, *dW = nullptr;
-    int* dinfo = nullptr;
-    void* dwork = nullptr;
-    size_t dwork_bytes = 0;
-    std::vector<char> hwork;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_eigvals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LuSmem)) !=
+            cudaSuccess)
+            return MSGPU_E_CUDA;
+        attr = true;
+    }
+    std::vector<int> hn(nitem), hd(nitem);
+    std::vector<size_t> hpos(nitem), hout(nitem);
+    std::vector<msgpu_model> hmodel(nitem);
+    size_t nout = 0;
+    for (int i = 0; i < nitem; ++i) {
+        const int mi = item_med ? item_med[i] : 0;
+        hn[i] = media[mi].n;
+        hd[i] = media[mi].d;
+        hpos[i] = med_pos[mi];
+        hmodel[i] = media[mi].model;
+        hout[i] = nout;
+        nout += (size_t)media[mi].n;
+    }
+    const size_t slot = (size_t)nmax * nmax;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return MSGPU_E_CUDA;
+    const size_t budget = free_b > ((size_t)4 << 30) ? free_b - ((size_t)4 << 30) : free_b / 2;
+    const int grid = (int)std::min<size_t>({(size_t)nitem, (size_t)2 * sms, std::max<size_t>(1, budget / (slot * 16))});
+    double *dpos = nullptr, *dks = nullptr;
+    zc *dmu = nullptr, *dwork = nullptr;
+    int *dn = nullptr, *dd = nullptr, *dst = nullptr;
+    size_t *dposo = nullptr, *douto = nullptr;
+    msgpu_model* dmodel = nullptr;
     auto cleanup = [&]() {
-        cudaFree(dpos); cudaFree(dA); cudaFree(dW); cudaFree(dinfo); cudaFree(dwork);
+        cudaFree(dpos); cudaFree(dks); cudaFree(dmu); cudaFree(dwork); cudaFree(dn); cudaFree(dd);
+        cudaFree(dst); cudaFree(dposo); cudaFree(douto); cudaFree(dmodel);
     };
-    size_t npos = 0;
-    for (int m = 0; m < nmed; ++m) npos = std::max(npos, (size_t)media[m].n * media[m].d);
-    if (cudaMalloc(&dpos, sizeof(double) * npos) || cudaMalloc(&dA, sizeof(zc) * (size_t)nmax * nmax) ||
-        cudaMalloc(&dW, sizeof(zc) * (size_t)nmax) || cudaMalloc(&dinfo, sizeof(int))) {
+    if (cudaMalloc(&dpos, sizeof(double) * npos) || cudaMalloc(&dks, sizeof(double) * 2 * nitem) ||
+        cudaMalloc(&dmu, sizeof(zc) * nout) || cudaMalloc(&dwork, sizeof(zc) * slot * grid) ||
+        cudaMalloc(&dn, sizeof(int) * nitem) || cudaMalloc(&dd, sizeof(int) * nitem) ||
+        cudaMalloc(&dst, sizeof(int) * nitem) || cudaMalloc(&dposo, sizeof(size_t) * nitem) ||
+        cudaMalloc(&douto, sizeof(size_t) * nitem) || cudaMalloc(&dmodel, sizeof(msgpu_model) * nitem)) {
         cleanup();
         return MSGPU_E_CUDA;
     }
-    size_t off = 0;
-    int last_med = -1;
-    for (int it = 0; it < nitem; ++it) {
-        const int mi = item_med ? item_med[it] : 0;
-        const msgpu_medium& md = media[mi];
-        const int n = md.n;
-        if (mi != last_med) {
-            if (cudaMemcpy(dpos, md.pos, sizeof(double) * (size_t)n * md.d, cudaMemcpyHostToDevice)) {
-                cleanup();
-                return MSGPU_E_CUDA;
-            }
-            last_med = mi;
-        }
-        const int nt = (n + 31) / 32;
-        k_build_matrix<<<std::min(nt, 4 * sms), NT, sizeof(LuSmem)>>>(dA, n, md.d, dpos, md.model, ks[2 * it],
-                                                                      ks[2 * it + 1], 0);
-        count_launches(1);
-        size_t need_d = 0, need_h = 0;
-        if (cudaGetLastError() != cudaSuccess ||
-            cusolverDnXgeev_bufferSize(g_solver, g_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_NOVECTOR, n,
-                                       CUDA_C_64F, dA, n, CUDA_C_64F, dW, CUDA_C_64F, nullptr, 1, CUDA_C_64F, nullptr,
-                                       1, CUDA_C_64F, &need_d, &need_h) != CUSOLVER_STATUS_SUCCESS) {
-            cleanup();
-            return MSGPU_E_CUDA;
-        }
-        if (need_d > dwork_bytes) {
-            cudaFree(dwork);
-            dwork = nullptr;
-            dwork_bytes = 0;
-            if (cudaMalloc(&dwork, need_d)) {
-                cleanup();
-                return MSGPU_E_CUDA;
-            }
-            dwork_bytes = need_d;
-        }
-        if (need_h > hwork.size()) hwork.resize(need_h);
-        if (cusolverDnXgeev(g_solver, g_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_NOVECTOR, n, CUDA_C_64F,
-                            dA, n, CUDA_C_64F, dW, CUDA_C_64F, nullptr, 1, CUDA_C_64F, nullptr, 1, CUDA_C_64F, dwork,
-                            dwork_bytes, hwork.empty() ? nullptr : hwork.data(), need_h,
-                            dinfo) != CUSOLVER_STATUS_SUCCESS) {
-            cleanup();
-            return MSGPU_E_CUDA;
-        }
-        int info = 0;
-        if (cudaMemcpy(mu + 2 * off, dW, sizeof(zc) * (size_t)n, cudaMemcpyDeviceToHost) ||
-            cudaMemcpy(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost)) {
-            cleanup();
-            return MSGPU_E_CUDA;
-        }
-        // info > 0: the QR algorithm left eigenvalues unconverged (eigvals' LAPACK warning)
-        if (status) status[it] = info > 0 ? MSGPU_S_NOCONV : 0;
-        off += (size_t)n;
+    bool ok = true;
+    for (int m = 0; m < nmed && ok; ++m)
+        ok = cudaMemcpy(dpos + med_pos[m], media[m].pos, sizeof(double) * (size_t)media[m].n * media[m].d,
+                        cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMemcpy(dks, ks, sizeof(double) * 2 * nitem, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(dn, hn.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(dd, hd.data(), sizeof(int) * nitem, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(dposo, hpos.data(), sizeof(size_t) * nitem, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(douto, hout.data(), sizeof(size_t) * nitem, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(dmodel, hmodel.data(), sizeof(msgpu_model) * nitem, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMemset(dmu, 0, sizeof(zc) * nout) == cudaSuccess;  // unconverged values read 0
+    if (!ok) {
+        cleanup();
+        return MSGPU_E_CUDA;
     }
+    EigParams P{nitem, dn, dd, dposo, dmodel, dpos, dks, douto, dmu, dst, dwork, slot};
+    k_eigvals<<<grid, NT, sizeof(LuSmem)>>>(P);
+    count_launches(1);
+    std::vector<int> hst(nitem);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(mu, dmu, sizeof(zc) * nout, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(hst.data(), dst, sizeof(int) * nitem, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cleanup();
+        return MSGPU_E_CUDA;
+    }
+    if (status)
+        for (int i = 0; i < nitem; ++i) status[i] = hst[i];
     cleanup();
     return 0;
 }

@@ -25,6 +25,29 @@ def test_eigvals_reference_runs(ms, ref_runs):
             want.pop(j)
 
 
+def _match_sets(mu, want, tol):
+    want = list(want)
+    scale = max(abs(w) for w in want)
+    for m in mu:  # greedy nearest matching, one to one
+        j = int(np.argmin([abs(m - w) for w in want]))
+        assert abs(m - want[j]) < tol * scale
+        want.pop(j)
+
+
+def test_eigvals_larger_against_oracle_matrix(ms, oracle):
+    """n = 200 (d = 3, complex k) and n = 129 (d = 2), a batch of three items on
+    two media: the kernel's eigenvalues against LAPACK zgeev (numpy) of the
+    oracle's M(k), within 1e-10 of the largest |mu|."""
+    cases = [(3, 200, 2.0 - 0.3j), (2, 129, 1.1 + 0.0j), (3, 200, 0.7 - 0.02j)]
+    media = [ms.Medium(3, 200, seed=4), ms.Medium(2, 129, seed=5)]
+    mus, st = ms.eigvals_batch(media, [c[2] for c in cases], item_med=[0, 1, 0])
+    assert np.all(st == 0)
+    for (d, n, k), mu, med in zip(cases, mus, [media[0], media[1], media[0]]):
+        assert len(mu) == n
+        want = np.linalg.eigvals(oracle.ms_matrix(d, n, med.pos, k))
+        _match_sets(mu, want, 1e-10)
+
+
 def test_run_chistogram_matches_reference(ms, ref_runs):
     """run_chistogram_omp end to end: the eigenvalues of M(k) of seeds 1..nseed
     on the GPU, binned as the reference bins its own (zgeev) eigenvalues.  The
