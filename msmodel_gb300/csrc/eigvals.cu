@@ -16,9 +16,8 @@
 //      subdiagonals, the Ahues-Kressner deflation test, Wilkinson shifts with
 //      exceptional shifts every 10 iterations without deflation, the search
 //      for two consecutive small subdiagonals, 2 x 2 reflectors chasing the
-//      bulge through the active block), run by the CTA's first warp: each
-//      bulge step is a chain of scalar work, and its row and column updates
-//      are split over the 32 lanes.
+//      bulge through the active block): thread 0 takes the scalar chain of
+//      each bulge step, the CTA splits the step's row and column updates.
 // zgeev also balances the matrix first (zgebal); this path does not: M(k)'s
 // entries do not span the magnitudes balancing is for, and the eigenvalues
 // agree with the reference's to ~1e-13 of the largest.  Eigenvalues come out
@@ -111,43 +110,63 @@ static __device__ void hessenberg(zc* __restrict__ A, int n, LuSmem& s) {
 }
 
 // zlarfg for n = 2: on return a = beta (real), x scaled, the reflector
-// I - tau (1, x)(1, x)^H
+// I - tau (1, x)(1, x)^H.  On the bulge-chasing chain of every QR step, so it
+// takes two divisions and one square root (zlarfg's dlapy3 scaling guards
+// against overflow of |a|^2 + |x|^2, far beyond M(k)'s entries)
 __device__ __forceinline__ zc larfg2(zc& a, zc& x) {
-    const double xnorm = zabs(x);
-    if (xnorm == 0.0 && a.im == 0.0) return mk(0.0);
-    const double beta = -copysign(dlapy3(a.re, a.im, xnorm), a.re);
-    const zc tau = mk((beta - a.re) / beta, -a.im / beta);
-    x = x * (1.0 / (a - beta));
+    const double x2 = zabs2(x);
+    if (x2 == 0.0 && a.im == 0.0) return mk(0.0);
+    const double beta = -copysign(sqrt(a.re * a.re + a.im * a.im + x2), a.re);
+    const double rb = 1.0 / beta;
+    const zc tau = mk((beta - a.re) * rb, -a.im * rb);
+    x = x * zrecip(a - beta);
     a = mk(beta);
     return tau;
 }
 
+// the QR iteration's scalars, computed by thread 0 and read by the CTA
+struct HqrShared {
+    zc t1, v2, temp;
+    double t2;
+    int l, m, flag;
+};
+
 // Eigenvalues of the upper Hessenberg H (n x n, ld n) into w by zlahqr's
-// single-shift QR (wantt = wantz = false); run by one warp, every lane taking
-// the same scalar path.  Returns 0, or i + 1 if eigenvalue i and above did not
-// converge within 30 max(10, n) iterations (zlahqr's info).
-static __device__ int hqr_warp(zc* __restrict__ H, int n, zc* __restrict__ w) {
-    const int lane = threadIdx.x & 31;
+// single-shift QR (wantt = wantz = false).  Thread 0 takes every scalar step
+// (the deflation and shift searches, each 2 x 2 reflector) and the CTA splits
+// each step's row and column updates, three barriers a bulge step.  (Letting
+// thread 0 update the next reflector's two rows itself and start on it while
+// the CTA finishes the step saves a barrier but measured 10-16% slower.)  Returns 0,
+// or i + 1 if eigenvalue i and above did not converge within 30 max(10, n)
+// iterations (zlahqr's info).
+static __device__ int hqr_cta(zc* __restrict__ H, int n, zc* __restrict__ w, HqrShared& q) {
+    const int tid = threadIdx.x;
     auto h = [&](int r, int c) -> zc& { return H[r + (size_t)c * n]; };
     if (n == 1) {
-        if (lane == 0) w[0] = h(0, 0);
+        if (tid == 0) w[0] = h(0, 0);
         return 0;
     }
     const int ilo = 0, ihi = n - 1;
     // subdiagonal entries made real by diagonal unitary similarity
     for (int i = ilo + 1; i <= ihi; ++i) {
-        const zc hs = h(i, i - 1);
-        __syncwarp();
-        if (hs.im != 0.0) {
-            zc sc = hs / abs1(hs);
-            sc = conjz(sc) / zabs(sc);
-            if (lane == 0) h(i, i - 1) = mk(zabs(hs));
-            for (int j = i + lane; j <= ihi; j += 32) h(i, j) = h(i, j) * sc;
-            __syncwarp();
-            const int top = min(ihi, i + 1);
-            for (int j = ilo + lane; j <= top; j += 32) h(j, i) = h(j, i) * conjz(sc);
+        if (tid == 0) {
+            const zc hs = h(i, i - 1);
+            q.flag = hs.im != 0.0;
+            if (q.flag) {
+                const zc sc = hs / abs1(hs);
+                q.temp = conjz(sc) / zabs(sc);
+                h(i, i - 1) = mk(zabs(hs));
+            }
         }
-        __syncwarp();
+        __syncthreads();
+        if (q.flag) {
+            const zc sc = q.temp;
+            for (int j = i + tid; j <= ihi; j += NT) h(i, j) = h(i, j) * sc;
+            __syncthreads();
+            const int top = min(ihi, i + 1);
+            for (int j = ilo + tid; j <= top; j += NT) h(j, i) = h(j, i) * conjz(sc);
+        }
+        __syncthreads();
     }
     const double safmin = DBL_MIN, ulp = DBL_EPSILON;
     const double smlnum = safmin * ((double)(ihi - ilo + 1) / ulp);
@@ -155,147 +174,168 @@ static __device__ int hqr_warp(zc* __restrict__ H, int n, zc* __restrict__ w) {
     constexpr int KEXSH = 10;
     int kdefl = 0;
     int i = ihi;
+    zc v0 = mk(0.0), v1 = mk(0.0);  // thread 0's reflector vector
     while (i >= ilo) {
         int l = ilo;
         bool done = false;
         for (int its = 0; its <= itmax; ++its) {
-            // a single small subdiagonal element
-            int k;
-            for (k = i; k > l; --k) {
-                const zc hkk1 = h(k, k - 1);
-                if (abs1(hkk1) <= smlnum) break;
-                double tst = abs1(h(k - 1, k - 1)) + abs1(h(k, k));
-                if (tst == 0.0) {
-                    if (k - 2 >= ilo) tst += fabs(h(k - 1, k - 2).re);
-                    if (k + 1 <= ihi) tst += fabs(h(k + 1, k).re);
+            if (tid == 0) {
+                // a single small subdiagonal element
+                int k;
+                for (k = i; k > l; --k) {
+                    const zc hkk1 = h(k, k - 1);
+                    if (abs1(hkk1) <= smlnum) break;
+                    double tst = abs1(h(k - 1, k - 1)) + abs1(h(k, k));
+                    if (tst == 0.0) {
+                        if (k - 2 >= ilo) tst += fabs(h(k - 1, k - 2).re);
+                        if (k + 1 <= ihi) tst += fabs(h(k + 1, k).re);
+                    }
+                    if (fabs(hkk1.re) <= ulp * tst) {
+                        const double a1 = abs1(hkk1), a2 = abs1(h(k - 1, k));
+                        const double ab = fmax(a1, a2), ba = fmin(a1, a2);
+                        const double b1 = abs1(h(k, k)), b2 = abs1(h(k - 1, k - 1) - h(k, k));
+                        const double aa = fmax(b1, b2), bb = fmin(b1, b2);
+                        const double sab = aa + ab;
+                        if (ba * (ab / sab) <= fmax(smlnum, ulp * (bb * (aa / sab)))) break;
+                    }
                 }
-                if (fabs(hkk1.re) <= ulp * tst) {
-                    const double a1 = abs1(hkk1), a2 = abs1(h(k - 1, k));
-                    const double ab = fmax(a1, a2), ba = fmin(a1, a2);
-                    const double b1 = abs1(h(k, k)), b2 = abs1(h(k - 1, k - 1) - h(k, k));
-                    const double aa = fmax(b1, b2), bb = fmin(b1, b2);
-                    const double sab = aa + ab;
-                    if (ba * (ab / sab) <= fmax(smlnum, ulp * (bb * (aa / sab)))) break;
+                if (k > ilo) h(k, k - 1) = mk(0.0);
+                q.l = k;
+                if (k < i) {
+                    const int kd = kdefl + 1;
+                    zc t;
+                    if (kd % (2 * KEXSH) == 0) {
+                        t = h(i, i) + 0.75 * fabs(h(i, i - 1).re);
+                    } else if (kd % KEXSH == 0) {
+                        t = h(k, k) + 0.75 * fabs(h(k + 1, k).re);
+                    } else {  // Wilkinson's shift
+                        t = h(i, i);
+                        const zc u = zsqrt(h(i - 1, i)) * zsqrt(h(i, i - 1));
+                        double s = abs1(u);
+                        if (s != 0.0) {
+                            const zc x = 0.5 * (h(i - 1, i - 1) - t);
+                            const double sx = abs1(x);
+                            s = fmax(s, sx);
+                            const zc xs = x / s, us = u / s;
+                            zc y = s * zsqrt(xs * xs + us * us);
+                            if (sx > 0.0) {
+                                const zc xn = x / sx;
+                                if (xn.re * y.re + xn.im * y.im < 0.0) y = -y;
+                            }
+                            t = t - u * (u / (x + y));
+                        }
+                    }
+                    // two consecutive small subdiagonal elements: start the sweep at row m
+                    int m;
+                    for (m = i - 1; m > k; --m) {
+                        const zc h11 = h(m, m), h22 = h(m + 1, m + 1);
+                        zc h11s = h11 - t;
+                        double h21 = h(m + 1, m).re;
+                        const double s = abs1(h11s) + fabs(h21);
+                        h11s = h11s / s;
+                        h21 /= s;
+                        v0 = h11s;
+                        v1 = mk(h21);
+                        const double h10 = h(m, m - 1).re;
+                        if (fabs(h10) * fabs(h21) <= ulp * (abs1(h11s) * (abs1(h11) + abs1(h22)))) break;
+                    }
+                    if (m == k) {
+                        const zc h11s = h(k, k) - t;
+                        const double h21 = h(k + 1, k).re;
+                        const double s = abs1(h11s) + fabs(h21);
+                        v0 = h11s / s;
+                        v1 = mk(h21 / s);
+                    }
+                    q.m = m;
                 }
             }
-            l = k;
-            __syncwarp();
-            if (l > ilo && lane == 0) h(l, l - 1) = mk(0.0);
-            __syncwarp();
+            __syncthreads();
+            l = q.l;
             if (l >= i) {
                 done = true;
                 break;
             }
             ++kdefl;
-            const int i1 = l, i2 = i;  // the active block
-            zc t;
-            if (kdefl % (2 * KEXSH) == 0) {
-                t = h(i, i) + 0.75 * fabs(h(i, i - 1).re);
-            } else if (kdefl % KEXSH == 0) {
-                t = h(l, l) + 0.75 * fabs(h(l + 1, l).re);
-            } else {  // Wilkinson's shift
-                t = h(i, i);
-                const zc u = zsqrt(h(i - 1, i)) * zsqrt(h(i, i - 1));
-                double s = abs1(u);
-                if (s != 0.0) {
-                    const zc x = 0.5 * (h(i - 1, i - 1) - t);
-                    const double sx = abs1(x);
-                    s = fmax(s, sx);
-                    const zc xs = x / s, us = u / s;
-                    zc y = s * zsqrt(xs * xs + us * us);
-                    if (sx > 0.0) {
-                        const zc xn = x / sx;
-                        if (xn.re * y.re + xn.im * y.im < 0.0) y = -y;
-                    }
-                    t = t - u * (u / (x + y));
-                }
-            }
-            // two consecutive small subdiagonal elements: start the sweep at row m
-            int m;
-            zc v0, v1;
-            for (m = i - 1; m > l; --m) {
-                const zc h11 = h(m, m), h22 = h(m + 1, m + 1);
-                zc h11s = h11 - t;
-                double h21 = h(m + 1, m).re;
-                const double s = abs1(h11s) + fabs(h21);
-                h11s = h11s / s;
-                h21 /= s;
-                v0 = h11s;
-                v1 = mk(h21);
-                const double h10 = h(m, m - 1).re;
-                if (fabs(h10) * fabs(h21) <= ulp * (abs1(h11s) * (abs1(h11) + abs1(h22)))) break;
-            }
-            if (m == l) {
-                const zc h11 = h(l, l);
-                zc h11s = h11 - t;
-                double h21 = h(l + 1, l).re;
-                const double s = abs1(h11s) + fabs(h21);
-                v0 = h11s / s;
-                v1 = mk(h21 / s);
-            }
+            const int i1 = l, i2 = i, m = q.m;
             // the single-shift QR sweep
             for (int kk = m; kk < i; ++kk) {
-                if (kk > m) {
-                    v0 = h(kk, kk - 1);
-                    v1 = h(kk + 1, kk - 1);
+                if (tid == 0) {
+                    if (kk > m) {
+                        v0 = h(kk, kk - 1);
+                        v1 = h(kk + 1, kk - 1);
+                    }
+                    const zc t1 = larfg2(v0, v1);
+                    if (kk > m) {
+                        h(kk, kk - 1) = v0;
+                        h(kk + 1, kk - 1) = mk(0.0);
+                    }
+                    q.t1 = t1;
+                    q.v2 = v1;
+                    q.t2 = (t1 * v1).re;
                 }
-                const zc t1 = larfg2(v0, v1);
-                __syncwarp();
-                if (kk > m && lane == 0) {
-                    h(kk, kk - 1) = v0;
-                    h(kk + 1, kk - 1) = mk(0.0);
-                }
-                const zc v2 = v1;
-                const double t2 = (t1 * v2).re;
+                __syncthreads();
+                const zc t1 = q.t1, v2 = q.v2;
+                const double t2 = q.t2;
                 // from the left: rows kk, kk+1, columns kk..i2
                 const zc ct1 = conjz(t1);
-                for (int j = kk + lane; j <= i2; j += 32) {
+                for (int j = kk + tid; j <= i2; j += NT) {
                     const zc sum = ct1 * h(kk, j) + t2 * h(kk + 1, j);
                     h(kk, j) -= sum;
                     h(kk + 1, j) -= sum * v2;
                 }
-                __syncwarp();
+                __syncthreads();
                 // from the right: columns kk, kk+1, rows i1..min(kk+2, i)
                 const zc cv2 = conjz(v2);
                 const int jt = min(kk + 2, i);
-                for (int j = i1 + lane; j <= jt; j += 32) {
+                for (int j = i1 + tid; j <= jt; j += NT) {
                     const zc sum = t1 * h(j, kk) + t2 * h(j, kk + 1);
                     h(j, kk) -= sum;
                     h(j, kk + 1) -= sum * cv2;
                 }
-                __syncwarp();
                 if (kk == m && m > l) {
-                    // the sweep started below l: keep H(m, m-1) real
+                    // the sweep started below l: keep H(m, m-1) real.  Row j in S =
+                    // [m, i] \ {m+1} takes temp right of the diagonal, column j in S takes
+                    // conj(temp) above it (zlahqr, one row and column at a time); an
+                    // entry in both keeps its value
                     zc temp = 1.0 - t1;
                     temp = temp / zabs(temp);
-                    if (lane == 0) {
+                    __syncthreads();
+                    if (tid == 0) {
                         h(m + 1, m) = h(m + 1, m) * conjz(temp);
                         if (m + 2 <= i) h(m + 2, m + 1) = h(m + 2, m + 1) * temp;
                     }
-                    __syncwarp();
-                    for (int j = m; j <= i; ++j) {
-                        if (j == m + 1) continue;
-                        for (int c = j + 1 + lane; c <= i2; c += 32) h(j, c) = h(j, c) * temp;
-                        for (int r = i1 + lane; r < j; r += 32) h(r, j) = h(r, j) * conjz(temp);
-                        __syncwarp();
+                    auto in_s = [&](int x) { return x >= m && x <= i && x != m + 1; };
+                    const int na = i - i1 + 1;
+                    for (int e = tid; e < na * na; e += NT) {
+                        const int r = i1 + e % na, c = i1 + e / na;
+                        if (r >= c) continue;
+                        const bool a = in_s(r), b = in_s(c);
+                        if (a && !b) h(r, c) = h(r, c) * temp;
+                        else if (b && !a) h(r, c) = h(r, c) * conjz(temp);
                     }
                 }
+                __syncthreads();
             }
             // H(i, i-1) made real
-            const zc temp = h(i, i - 1);
-            __syncwarp();
-            if (temp.im != 0.0) {
-                const double rt = zabs(temp);
-                const zc u = temp / rt;
-                if (lane == 0) h(i, i - 1) = mk(rt);
-                for (int c = i + 1 + lane; c <= i2; c += 32) h(i, c) = h(i, c) * conjz(u);
-                for (int r = i1 + lane; r < i; r += 32) h(r, i) = h(r, i) * u;
+            if (tid == 0) {
+                const zc temp = h(i, i - 1);
+                q.flag = temp.im != 0.0;
+                if (q.flag) {
+                    const double rt = zabs(temp);
+                    q.temp = temp / rt;
+                    h(i, i - 1) = mk(rt);
+                }
             }
-            __syncwarp();
+            __syncthreads();
+            if (q.flag) {
+                const zc u = q.temp;
+                for (int c = i + 1 + tid; c <= i2; c += NT) h(i, c) = h(i, c) * conjz(u);
+                for (int r = i1 + tid; r < i; r += NT) h(r, i) = h(r, i) * u;
+            }
+            __syncthreads();
         }
         if (!done) return i + 1;
-        if (lane == 0) w[i] = h(i, i);
-        __syncwarp();
+        if (tid == 0) w[i] = h(i, i);
         kdefl = 0;
         i = l - 1;
     }
@@ -305,6 +345,7 @@ static __device__ int hqr_warp(zc* __restrict__ H, int n, zc* __restrict__ w) {
 __global__ void __launch_bounds__(NT, 2) k_eigvals(EigParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LuSmem& s = *reinterpret_cast<LuSmem*>(smem_raw);
+    __shared__ HqrShared q;
     zc* A = P.work + (size_t)blockIdx.x * P.slot;
     for (int it = blockIdx.x; it < P.nitem; it += gridDim.x) {
         const int n = P.item_n[it];
@@ -312,8 +353,7 @@ __global__ void __launch_bounds__(NT, 2) k_eigvals(EigParams P) {
         assemble(A, nullptr, n, P.item_d[it], P.pos + P.item_pos[it], P.item_model[it], k, s);
         __syncthreads();
         hessenberg(A, n, s);
-        int info = 0;
-        if (threadIdx.x < 32) info = hqr_warp(A, n, P.mu + P.item_out[it]);
+        const int info = hqr_cta(A, n, P.mu + P.item_out[it], q);
         if (threadIdx.x == 0) P.status[it] = info > 0 ? MSGPU_S_NOCONV : 0;
         __syncthreads();
     }
