@@ -24,7 +24,8 @@ sample = 4096).  One step = the hot path over the whole cut.
            its accuracy against FP64 and the oracle, and a CPU baseline
 
 Other configurations print one line each with --workload map64 | map2d |
-aberth | wave.
+aberth | wave; --workload eigvals times the eigenvalues of M(k) behind the
+mu-plane histograms (batches at n = 128, 256, 512) against LAPACK zgeev.
 
 Multi-GPU (torchrun): weak scaling by default -- each rank evaluates the full
 cut for its own realisation (seed = rank + 1); --scaling strong splits the
@@ -592,7 +593,70 @@ def config_legs(ms, torch, no_cpu):
     return legs
 
 
-WORKLOADS = {"map64": workload_map64, "map2d": workload_map2d, "aberth": workload_aberth, "wave": workload_wave}
+_ZGEEV_TIMER = r"""
+import json, os, sys, time
+import numpy as np
+sys.path.insert(0, os.getcwd())
+from oracle import Oracle
+o = Oracle()
+out = {}
+for n, reps in ((128, 4), (256, 4), (512, 2)):
+    mats = [o.ms_matrix(3, n, o.fill_medium(3, n, s + 1), 1.3 + 0j) for s in range(reps)]
+    t0 = time.perf_counter()
+    for m in mats:
+        np.linalg.eigvals(m)
+    out[n] = (time.perf_counter() - t0) / reps
+print(json.dumps(out))
+"""
+
+
+def workload_eigvals(ms, torch, args):
+    """Eigenvalues of M(k) (eigvals, zgeev) for the mu-plane histograms: batches
+    of `count` d=3 realisations at n = 128, 256, 512 (k = 1.3) through the
+    public call (positions in, eigenvalues out), checked against LAPACK zgeev
+    (numpy) on the first two matrices of each batch; the CPU baseline is that
+    zgeev, one matrix per core (OPENBLAS_NUM_THREADS=1), as the reference's
+    OpenMP loop over realisations runs it."""
+    from oracle import Oracle
+    count = args.count or 304
+    res = {}
+    for n in (128, 256, 512):
+        media = [ms.Medium(3, n, seed=s) for s in range(1, 9)]
+        im = (np.arange(count) % len(media)).astype(np.int32)
+        ks = np.full(count, 1.3 + 0.0j)
+        ms.eigvals_batch(media[:1], ks[:1], np.zeros(1, dtype=np.int32))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mus, st = ms.eigvals_batch(media, ks, im)
+        dt = time.perf_counter() - t0
+        err = 0.0
+        for j in range(2):
+            want = list(np.linalg.eigvals(Oracle().ms_matrix(3, n, media[j].pos, 1.3 + 0j)))
+            scale = max(abs(w) for w in want)
+            for m in mus[j]:
+                i = int(np.argmin([abs(m - w) for w in want]))
+                err = max(err, abs(m - want[i]) / scale)
+                want.pop(i)
+        res[n] = {"matrices_per_s": count / dt, "seconds": dt, "nonconverged": int(np.count_nonzero(st)),
+                  "max_rel_err_vs_zgeev": err}
+    cpu = None
+    if not args.no_cpu:
+        env = dict(os.environ, OPENBLAS_NUM_THREADS="1")
+        r = subprocess.run([sys.executable, "-c", _ZGEEV_TIMER], capture_output=True, text=True, env=env, check=True)
+        per = {int(k): v for k, v in json.loads(r.stdout.strip().splitlines()[-1]).items()}
+        th = os.cpu_count() or 1
+        cpu = {"value": {str(n): th / per[n] for n in per}, "unit": "matrices/s", "cores": th, "kind": "port",
+               "sample": "LAPACK zgeev (numpy's OpenBLAS, 1 thread) on the oracle's M(k): 4 matrices at n=128 and "
+                         "256, 2 at n=512, seconds per matrix times the cores (one matrix per core)",
+               "seconds_per_matrix_1core": {str(n): per[n] for n in per}}
+    return {**({"cpu_baseline": cpu} if cpu else {}),
+            "workload": f"eigvals d=3 k=1.3, batches of {count} realisations at n=128,256,512", "unit": "matrices/s",
+            "gpu": {str(n): res[n] for n in res}, "gpu_launches_per_batch": 1,
+            "data": "synthetic (seeded scatterers drawn by the reference's generator)"}
+
+
+WORKLOADS = {"map64": workload_map64, "map2d": workload_map2d, "aberth": workload_aberth, "wave": workload_wave,
+             "eigvals": workload_eigvals}
 
 
 def run_workload(args):
@@ -671,7 +735,7 @@ def main():
                     help="skip the compact C1/C3/C5 legs of the default line")
     ap.add_argument("--workload", default="cut", choices=["cut"] + sorted(WORKLOADS),
                     help="cut: the headline line; others: one measurement line of that configuration")
-    ap.add_argument("--count", type=int, default=0, help="aberth workload: realisations (default 4096)")
+    ap.add_argument("--count", type=int, default=0, help="aberth workload: realisations (default 4096); eigvals: matrices per batch (default 304)")
     ap.add_argument("--fp64-count", type=int, default=64, help="aberth workload: realisations searched in FP64")
     ap.add_argument("--nk-wave", type=int, default=256, help="wave workload: wave numbers")
     ap.add_argument("--legs", default="mixed,fp64", help="wave workload: precisions to run")
