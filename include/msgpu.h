@@ -228,9 +228,12 @@ int msgpu_inverse_iteration_batch(int nmed, const msgpu_medium* media, int nitem
  * eigenvalue of M(k) or on 1/tr M(k)^-1; all function values of one step, over
  * every root and medium, in one batched GPU job.  Non-converged roots dropped,
  * duplicates (relative 1e-14) removed, order kept: roots[2*(m*nz + i)],
- * nroots[m]; *nevals (may be NULL) the function evaluations.  mineigval starts
- * every inverse iteration from the constant unit vector (the reference reuses
- * the previous call's eigenvector). */
+ * nroots[m]; *nevals (may be NULL) the function evaluations.  mineigval chains
+ * one eigenvector through every evaluation of a realisation, as the reference
+ * does (ms_core.c:339-340): each inverse iteration starts from the vector the
+ * previous one returned, roots in the reference's order (including the check of
+ * f at each root, ms_core.c:356), from the constant unit vector at the start;
+ * the batch is over the realisations. */
 int msgpu_find_roots_muller_batch(int method, int nmed, const msgpu_medium* media, const double* dom, int nz,
                                   const double* z0, int maxit, double toler, int precision, double* roots,
                                   int* nroots, int* nevals);
