@@ -384,13 +384,10 @@ extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nite
     const int sms = msgpu_sm_count();  // initialises the device and the kernels' attributes
     if (sms < 1) return MSGPU_E_NODEV;
     std::lock_guard<std::mutex> lk(g_eig_mu);
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(k_eigvals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LuSmem)) !=
-            cudaSuccess)
-            return MSGPU_E_CUDA;
-        attr = true;
-    }
+    // on every call: the attribute belongs to the current device
+    if (cudaFuncSetAttribute(k_eigvals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LuSmem)) !=
+        cudaSuccess)
+        return MSGPU_E_CUDA;
     std::vector<int> hn(nitem), hd(nitem);
     std::vector<size_t> hpos(nitem), hout(nitem);
     std::vector<msgpu_model> hmodel(nitem);

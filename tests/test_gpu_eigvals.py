@@ -48,6 +48,18 @@ def test_eigvals_larger_against_oracle_matrix(ms, oracle):
         _match_sets(mu, want, 1e-10)
 
 
+def test_eigvals_tiny_matrices(ms, oracle):
+    """n = 1 (the QR returns the diagonal), 2 (no Householder step) and 3 (one),
+    against LAPACK on the oracle's M(k)."""
+    media = [ms.Medium(3, n, seed=7) for n in (1, 2, 3)]
+    k = 0.9 - 0.1j
+    mus, st = ms.eigvals_batch(media, [k] * 3, item_med=[0, 1, 2])
+    assert np.all(st == 0)
+    for n, mu, med in zip((1, 2, 3), mus, media):
+        assert len(mu) == n
+        _match_sets(mu, np.linalg.eigvals(oracle.ms_matrix(3, n, med.pos, k)), 1e-12)
+
+
 def test_run_chistogram_matches_reference(ms, ref_runs):
     """run_chistogram_omp end to end: the eigenvalues of M(k) of seeds 1..nseed
     on the GPU, binned as the reference bins its own (zgeev) eigenvalues.  The
