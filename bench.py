@@ -149,16 +149,23 @@ def oracle_cut(o):
     return ks, o.fill_medium(D, N, 1)
 
 
-def strided_sample(ks, step, per_step, stride=128):
-    """`per_step` cut points for step `step`, strided across the whole cut:
-    offsets step, step + stride, ... (mod stride), so that successive steps
-    walk every residue class and the sample spans Re k in [0.5, 3]."""
+def strided_indices(nk, step, per_step, stride=128):
+    """`per_step` indices of cut points for step `step`, strided across the
+    whole cut: offsets step, step + stride, ... (mod stride), so that successive
+    steps walk every residue class and the sample spans Re k in [0.5, 3]."""
     out = []
     r = step
     while len(out) < per_step:
-        out.extend(ks[r % stride::stride][: per_step - len(out)])
+        out.extend(range(r % stride, nk, stride)[: per_step - len(out)])
         r += 1
     return np.asarray(out)
+
+
+def strided_sample(ks, step, per_step, stride=128):
+    return ks[strided_indices(len(ks), step, per_step, stride)]
+
+
+_ORACLE_SAMPLE = {}
 
 
 def cpu_baseline(seconds=15.0):
@@ -171,14 +178,18 @@ def cpu_baseline(seconds=15.0):
     ks, pos = oracle_cut(o)
     per_chunk = 2 * threads
     done, t0, i = 0, time.perf_counter(), 0
+    idx, vals = [], []
     while True:
-        chunk = strided_sample(ks, i, per_chunk)
-        o.tracelog_batch(D, N, pos, chunk, nthreads=threads)
-        done += len(chunk)
+        ix = strided_indices(len(ks), i, per_chunk)
+        vals.append(o.tracelog_batch(D, N, pos, ks[ix], nthreads=threads)[0])
+        idx.append(ix)
+        done += len(ix)
         i += 1
         el = time.perf_counter() - t0
         if el >= seconds and i >= 2:
             break
+    # the oracle's values, for the GPU engines' error on these points (taken out of the line)
+    _ORACLE_SAMPLE["idx"], _ORACLE_SAMPLE["values"] = np.concatenate(idx), np.concatenate(vals)
     return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{done} of the 4096 cut points taken every 128th across the cut (offsets 0..{i - 1}), "
                       f"N=1024 d=3 seed 1, {threads} OpenMP threads x 1 OpenBLAS thread "
@@ -225,8 +236,8 @@ def measure_mixed(ms, torch, med, ks, out64, args, stream, flush, ws, barrier):
     # bf16 tensor work actually executed: 40 real n x n x 32 slice products per
     # 32-column panel step (4 real products x 10 slice pairs), i.e. 80/3 n^3 flops
     tensor_flops = 80.0 / 3.0 * n ** 3 * len(ks) / (tot / args.steps)
-    return {"value": value, "unit": UNIT, "ms_per_step": 1e3 * tot / args.steps, "gpu_launches": launches,
-            "ratio_vs_fp64": None,
+    return {"_out": outm, "value": value, "unit": UNIT, "ms_per_step": 1e3 * tot / args.steps,
+            "gpu_launches": launches, "ratio_vs_fp64": None,
             "e2e": {"value": len(ks) * ws / e_el, "unit": UNIT, "steps": 1},
             "lndet_rel_err_vs_fp64": {"max": float(relerr.max()), "median": float(np.median(relerr)),
                                       "points": int(relerr.size)},
@@ -859,6 +870,15 @@ def main():
 
     if mixed:
         mixed["ratio_vs_fp64"] = mixed["value"] / value
+    outm = mixed.pop("_out") if mixed else None
+    if cpu and _ORACLE_SAMPLE and natom == N and len(out) == NK:
+        # the engines against the oracle on the cut points its CPU leg evaluated
+        ix, ref = _ORACLE_SAMPLE["idx"], _ORACLE_SAMPLE["values"]
+        rel = lambda v: np.abs((v[ix] - ref).real) / np.abs(ref.real)
+        cmp = {args.precision: out, **({"mixed": outm} if outm is not None else {})}
+        cpu["lndet_rel_err_vs_oracle"] = {"points": int(ix.size),
+                                          **{f"{k}_max": float(rel(v).max()) for k, v in cmp.items()},
+                                          **{f"{k}_median": float(np.median(rel(v))) for k, v in cmp.items()}}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
