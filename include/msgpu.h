@@ -250,6 +250,16 @@ int msgpu_find_roots_muller_batch(int method, int nmed, const msgpu_medium* medi
 int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med, const double* ks,
                         double* mu, int* status);
 
+/* The same for the matrix type of the mu-plane task (mtype in run_chistogram_omp,
+ * ms_core.c:173-232): MSGPU_MTYPE_MSMATRIX, M(k), as msgpu_eigvals_batch; or
+ * MSGPU_MTYPE_NORMALIZED, N(k) = i - G(k)/I(k,0) with I(k,0) = -Im G(k, 0)
+ * (build_normalized_matrix, ms_matrix_util.c:50), independent of the
+ * scattering model. */
+#define MSGPU_MTYPE_MSMATRIX 0
+#define MSGPU_MTYPE_NORMALIZED 1
+int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
+                              const double* ks, double* mu, int* status);
+
 /* Launch choices (autotuning).  Per (kind, requested precision, size bucket
  * of the job's largest n: (2^(b-1), 2^b]) the engine that runs and the
  * resident CTAs per SM of the persistent grid.  engine: MSGPU_FP64,

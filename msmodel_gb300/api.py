@@ -11,6 +11,8 @@ import ctypes as C
 import warnings
 import os
 
+import math
+
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -89,6 +91,7 @@ def lib():
     L.msgpu_find_roots_muller_batch.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), _dp, C.c_int, _dp, C.c_int,
                                                 C.c_double, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
     L.msgpu_eigvals_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip]
+    L.msgpu_eigvals_batch_mtype.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip]
     L.msgpu_tune_set.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.msgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.msgpu_autotune.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
@@ -482,14 +485,19 @@ def inverse_iteration_batch(media, ks, item_med=None, want_vecs=True):
     return lam.view(np.complex128).copy(), parts, st
 
 
-def eigvals_batch(media, ks, item_med=None):
-    """The n eigenvalues of M(k) per item (eigvals, ms_matrix_util.c:147):
-    (list of arrays, status)."""
+MTYPES = {"msmatrix": 0, "normalized": 1}
+
+
+def eigvals_batch(media, ks, item_med=None, mtype="msmatrix"):
+    """The n eigenvalues per item (eigvals, ms_matrix_util.c:147) of M(k), or
+    with mtype "normalized" of N(k) = i - G(k)/I(k,0) (build_normalized_matrix,
+    ms_matrix_util.c:50): (list of arrays, status)."""
     media = [media] if isinstance(media, Medium) else list(media)
     kk, nitem, im = _items(media, ks, item_med)
     mu = np.zeros(2 * sum(media[i].n for i in im))
     st = np.zeros(nitem, dtype=np.int32)
-    _check(lib().msgpu_eigvals_batch(len(media), _media_array(media), nitem, im, kk, mu, st), "eigvals_batch")
+    _check(lib().msgpu_eigvals_batch_mtype(MTYPES[mtype], len(media), _media_array(media), nitem, im, kk, mu, st),
+           "eigvals_batch")
     mu = mu.view(np.complex128)
     out, off = [], 0
     for i in im:
@@ -520,11 +528,35 @@ def imag_mu_histogram(mus, nbin, xmin, xmax):
     return dens, centres, lost
 
 
+def _c_round(v):
+    """C's round(): halves away from zero (numpy rounds them to even)."""
+    v = np.asarray(v, dtype=np.float64)
+    r = np.trunc(v)
+    return r + np.where(np.abs(v - r) >= 0.5, np.sign(v), 0.0)
+
+
+def _c_log(v):
+    """The C library's log (math.log calls it), with its results for v <= 0."""
+    v = float(v)
+    if v > 0.0 or v != v:
+        return math.log(v) if v == v else v
+    return -math.inf if v == 0.0 else -math.nan
+
+
+def _c_exp(v):
+    v = float(v)
+    try:
+        return math.exp(v)
+    except OverflowError:
+        return math.inf
+
+
 def chistogram(mus, xbin, ybin, mbin, dom=None, mrange=None):
     """The mu-plane histogram of run_chistogram_omp (ms_core.c:173-232) from the
     eigenvalues of every realisation, binned as fill_chist does
     (chistogram_util.c:103-264):
-      * moments: the mean and the per-component standard deviation of mu;
+      * moments: the mean and the per-component standard deviation of mu,
+        summed in order as the reference sums them;
       * domain {xmin, xmax, ymin, ymax}: given, or the extremes of the values;
         pixel (ix, iy) = (round((xbin-1)(Re mu - xmin)/(xmax - xmin)),
         round((ybin-1)(ymax - Im mu)/(ymax - ymin))), row-major from the top
@@ -538,42 +570,50 @@ def chistogram(mus, xbin, ybin, mbin, dom=None, mrange=None):
     z = np.concatenate([np.asarray(m, dtype=np.complex128).ravel() for m in mus])
     if z.size < 2:
         raise ValueError("chistogram: at least two values are needed to set up the domain")
-    avg = z.mean()
-    dz = z - avg
-    sigma = complex(np.sqrt(np.mean(dz.real ** 2)), np.sqrt(np.mean(dz.imag ** 2)))
+    # stat_moments (chistogram_util.c:103-121): sums in order, as the reference
+    # adds them (cumsum is sequential), so that the moments match its bits
+    nz = z.size
+    avg = complex(np.cumsum(z.real)[-1] / nz, np.cumsum(z.imag)[-1] / nz)
+    dzr, dzi = z.real - avg.real, z.imag - avg.imag
+    sigma = complex(np.sqrt(np.cumsum(dzr * dzr)[-1] / nz), np.sqrt(np.cumsum(dzi * dzi)[-1] / nz))
     if dom is None:
         dom = [float(z.real.min()), float(z.real.max()), float(z.imag.min()), float(z.imag.max())]
     if mrange is None:
         mrange = [float(z.imag.min()), float(z.imag.max())]
     xmin, xmax, ymin, ymax = dom
     with np.errstate(divide="ignore", invalid="ignore"):
-        ix = np.round((xbin - 1) * (z.real - xmin) / (xmax - xmin))
-        iy = np.round((ybin - 1) * (ymax - z.imag) / (ymax - ymin))
+        ix = _c_round((xbin - 1) * (z.real - xmin) / (xmax - xmin))
+        iy = _c_round((ybin - 1) * (ymax - z.imag) / (ymax - ymin))
     ok = np.isfinite(ix) & np.isfinite(iy) & (ix >= 0) & (ix < xbin) & (iy >= 0) & (iy < ybin)
     data = np.zeros(xbin * ybin)
     np.add.at(data, (ix[ok] + iy[ok] * xbin).astype(np.int64), 1.0)
     lost = int(z.size - ok.sum())
+    # the marginal with the C library's log and exp, as the reference's
+    # append_to_marginal and normalize_marginal_chist (chistogram_util.c:210-249) call them
     mmin, mmax = mrange
+    lmin, lmax = _c_log(mmin), _c_log(mmax)
     with np.errstate(divide="ignore", invalid="ignore"):
-        lmin, lmax = np.log(mmin), np.log(mmax)
-        im = np.round((mbin - 1) * (np.log(z.imag) - lmin) / (lmax - lmin))
+        im = _c_round((mbin - 1) * (np.array([_c_log(v) for v in z.imag]) - lmin) / (lmax - lmin))
     okm = np.isfinite(im) & (im >= 0) & (im < mbin)
     mdata = np.zeros(mbin)
     np.add.at(mdata, im[okm].astype(np.int64), 1.0)
     lost += int(z.size - okm.sum())
+    total = float(np.cumsum(mdata)[-1])
+    fac = _c_log(mmax / mmin) / (mbin - 1) if mmin != 0 else math.nan
     with np.errstate(divide="ignore", invalid="ignore"):
-        fac = np.log(mmax / mmin) / (mbin - 1)
-        x = mmin * np.exp(fac * np.arange(mbin))
-        mdata = mdata / (fac * x * mdata.sum())
-    return {"data": data.reshape(ybin, xbin), "mdata": mdata, "dom": dom, "mrange": mrange, "avg": complex(avg),
+        for i in range(mbin):
+            x = mmin * _c_exp(fac * i)
+            mdata[i] = mdata[i] / (fac * x * total)
+    return {"data": data.reshape(ybin, xbin), "mdata": mdata, "dom": dom, "mrange": mrange, "avg": avg,
             "sigma": sigma, "lost": lost}
 
 
-def run_chistogram(media, k, xbin, ybin, mbin, dom=None, mrange=None):
-    """run_chistogram_omp (ms_core.c:173-232): the eigenvalues of M(k) of every
-    realisation on the GPU (eigvals_batch), binned by chistogram."""
+def run_chistogram(media, k, xbin, ybin, mbin, dom=None, mrange=None, mtype="msmatrix"):
+    """run_chistogram_omp (ms_core.c:173-232): the eigenvalues of M(k) (or of
+    N(k), mtype "normalized") of every realisation on the GPU (eigvals_batch),
+    binned by chistogram."""
     media = [media] if isinstance(media, Medium) else list(media)
-    mus, st = eigvals_batch(media, np.full(len(media), complex(k)), np.arange(len(media), dtype=np.int32))
+    mus, st = eigvals_batch(media, np.full(len(media), complex(k)), np.arange(len(media), dtype=np.int32), mtype)
     out = chistogram(mus, xbin, ybin, mbin, dom, mrange)
     out["status"] = st
     return out

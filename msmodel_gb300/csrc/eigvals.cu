@@ -5,7 +5,9 @@
 //
 // One persistent CTA per matrix slot, FP64 throughout (the reference's
 // arithmetic), items dealt to CTAs in order:
-//   1. M(k) assembled by the FP64 engine's assembly (lu64.cuh);
+//   1. M(k) assembled by the FP64 engine's assembly (lu64.cuh), or the
+//      normalized N(k) = i - G(k)/I(k,0) of the mu-plane task's mtype=normalized
+//      (build_normalized_matrix, ms_matrix_util.c:50) made from it in place;
 //   2. reduction to upper Hessenberg form by Householder reflectors, as
 //      LAPACK's unblocked zgehd2 (reflector of zlarfg; H applied from the
 //      right to rows 0..n-1, H^H from the left to the trailing rows), the
@@ -50,6 +52,7 @@ struct EigParams {
     int* status;
     zc* work;                // one nmax x nmax slot per CTA
     size_t slot;
+    int normalized;          // N(k) = i - G(k)/I(k,0) in place of M(k)
 };
 
 __device__ __forceinline__ double dlapy3(double x, double y, double z) {
@@ -352,6 +355,18 @@ __global__ void __launch_bounds__(NT, 2) k_eigvals(EigParams P) {
         const zc k = mk(P.ks[2 * it], P.ks[2 * it + 1]);
         assemble(A, nullptr, n, P.item_d[it], P.pos + P.item_pos[it], P.item_model[it], k, s);
         __syncthreads();
+        if (P.normalized) {
+            // build_normalized_matrix (ms_matrix_util.c:50): off the diagonal -G(k, r_ij) / I(k, 0),
+            // that is M_ij / I(k, 0); i on the diagonal
+            if (threadIdx.x == 0) s.diag[0] = free_green_imag(P.item_d[it], k, 0.0);
+            __syncthreads();
+            const zc iz = s.diag[0];
+            for (size_t e = threadIdx.x; e < (size_t)n * n; e += NT) {
+                const size_t r = e % n, c = e / n;
+                A[e] = r == c ? mk(0.0, 1.0) : A[e] / iz;
+            }
+            __syncthreads();
+        }
         hessenberg(A, n, s);
         const int info = hqr_cta(A, n, P.mu + P.item_out[it], q);
         if (threadIdx.x == 0) P.status[it] = info > 0 ? MSGPU_S_NOCONV : 0;
@@ -365,10 +380,12 @@ namespace {
 std::mutex g_eig_mu;
 }
 
-extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med,
-                                   const double* ks, double* mu, int* status) {
+extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium* media, int nitem,
+                                         const int* item_med, const double* ks, double* mu, int* status) {
     using namespace msg;
-    if (nmed < 1 || !media || nitem < 1 || !ks || !mu) return MSGPU_E_ARG;
+    if ((mtype != MSGPU_MTYPE_MSMATRIX && mtype != MSGPU_MTYPE_NORMALIZED) || nmed < 1 || !media || nitem < 1 || !ks ||
+        !mu)
+        return MSGPU_E_ARG;
     int nmax = 0;
     size_t npos = 0;
     std::vector<size_t> med_pos(nmed);
@@ -438,7 +455,8 @@ extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nite
         cleanup();
         return MSGPU_E_CUDA;
     }
-    EigParams P{nitem, dn, dd, dposo, dmodel, dpos, dks, douto, dmu, dst, dwork, slot};
+    EigParams P{nitem, dn, dd, dposo, dmodel, dpos, dks, douto, dmu, dst, dwork, slot,
+                mtype == MSGPU_MTYPE_NORMALIZED};
     k_eigvals<<<grid, NT, sizeof(LuSmem)>>>(P);
     count_launches(1);
     std::vector<int> hst(nitem);
@@ -452,4 +470,9 @@ extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nite
         for (int i = 0; i < nitem; ++i) status[i] = hst[i];
     cleanup();
     return 0;
+}
+
+extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med,
+                                   const double* ks, double* mu, int* status) {
+    return msgpu_eigvals_batch_mtype(MSGPU_MTYPE_MSMATRIX, nmed, media, nitem, item_med, ks, mu, status);
 }

@@ -13,16 +13,20 @@ appends the section it names with the same keys, order and number formats:
   [eigenstate_list]  save_eigenstate_list  src/core/eigenstate_list_util.c:296-314
                      (domain: save_domain, domain_util.c:83; states: save_eigenstate,
                      eigenstate_util.c:202-213)
+  [muplane]          save_chistogram       src/core/chistogram_util.c:414-440
+                     (domain: save_domain; color line: save_colorrule)
   data= line         save_cdata            src/core/complex_data_util.c:21-28
 
 `parse_cdata` reads a data= line back (parse_complex_data,
 src/core/complex_vector_util.c:215-231).  Numbers go through C-style printf
 conversions (%g, %.16g, %+.16g), which Python's % operator reproduces.
 """
+import math
+
 import numpy as np
 
 __all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
-           "save_random_function", "save_eigenstate_list"]
+           "save_random_function", "save_eigenstate_list", "save_muplane"]
 
 MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
@@ -48,6 +52,14 @@ def parse_cdata(line, n=None):
         if n is not None and len(out) == n:
             break
     return np.asarray(out, dtype=np.complex128)
+
+
+def _g16(v):
+    """%.16g as glibc's printf writes it, NaN with its sign ("-nan") included."""
+    v = float(v)
+    if v != v:
+        return "-nan" if math.copysign(1.0, v) < 0 else "nan"
+    return "%.16g" % v
 
 
 def _append(fname, text):
@@ -103,3 +115,27 @@ def save_eigenstate_list(fname, states, seed, method, ntarget, dom, maxit, toler
         text += "st%d_mu=%.16g%+.16gi\n" % (i, mu.real, mu.imag)
         text += "st%d_eigv=" % i + "".join("%.16g%+.16gi " % (z.real, z.imag) for z in np.asarray(v)) + "\n"
     _append(fname, text + "\n")
+
+
+def save_muplane(fname, hist, k, nseed, mtype="msmatrix", title="", color=("magma", "seq", 3.0, False),
+                 realtime=0.0):
+    """A [muplane] section for the mu-plane histogram hist (the dict chistogram /
+    run_chistogram return) of the eigenvalues of M(k) (mtype "msmatrix") or of
+    N(k) (mtype "normalized") over nseed realisations.  color = (map name, "seq"
+    or "div", contrast, reversed), the reference's default being magma seq 3."""
+    k = complex(k)
+    xmin, xmax, ymin, ymax = hist["dom"]
+    name, ctype, ctr, rev = color
+    text = "[muplane]\ntitle=%s\nmtype=%s\nk=%.16g%+.16gi\nnseed=%d\n" % (title, mtype, k.real, k.imag, nseed)
+    data = np.asarray(hist["data"]).reshape(-1)
+    ybin, xbin = np.asarray(hist["data"]).shape
+    text += "xbin=%d\nybin=%d\n" % (xbin, ybin)
+    text += "xrange=%.16g:%.16g\nyrange=%.16g:%.16g\n" % (xmin, xmax, ymin, ymax)
+    avg, sig = complex(hist["avg"]), complex(hist["sigma"])
+    text += "avgz=%.16g%+.16gi\nsigmaz=%.16g%+.16gi\n" % (avg.real, avg.imag, sig.real, sig.imag)
+    text += "realtime=%g\ncolor=%s %s %g%s\n" % (realtime, name, ctype, ctr, " rev" if rev else "")
+    text += "data=" + "".join(_g16(v) + " " for v in data) + "\n"
+    mdata = np.asarray(hist["mdata"])
+    text += "mbin=%d\nmrange=%.16g:%.16g\n" % (mdata.size, hist["mrange"][0], hist["mrange"][1])
+    text += "mdata=" + "".join(_g16(v) + " " for v in mdata) + "\n\n"
+    _append(fname, text)

@@ -242,6 +242,9 @@ class Reference:
         L.ref_traceinv.argtypes = med + [C.c_int, _dp, _dp]
         L.ref_eigvals.argtypes = med + [_dp, _dp]
         L.ref_chistogram.argtypes = [C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.ref_eigvals_normalized.argtypes = med + [_dp, _dp]
+        L.ref_save_chistogram.argtypes = [C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.c_char_p, C.c_char_p, C.c_double, C.c_char_p]
         L.ref_inverse_iteration.argtypes = med + [_dp, _dp, _dp]
         L.ref_roots_muller.argtypes = [C.c_int] + med + [_dp, C.c_int, _dp, C.c_int, C.c_double]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
@@ -296,6 +299,25 @@ class Reference:
         mu = np.zeros(2 * n)
         self.L.ref_eigvals(*self._med(d, n, model, params, shape, ratio, seed), np.array([k.real, k.imag]), mu)
         return mu.view(np.complex128).copy()
+
+    def eigvals_normalized(self, d, n, seed, k, model="maximum", params=(), shape="ball", ratio=1.0):
+        """eigvals of the normalized MS matrix N(k) = i - G(k)/I(k,0) (build_normalized_matrix)."""
+        mu = np.zeros(2 * n)
+        self.L.ref_eigvals_normalized(*self._med(d, n, model, params, shape, ratio, seed),
+                                      np.array([k.real, k.imag]), mu)
+        return mu.view(np.complex128).copy()
+
+    def save_chistogram(self, mu, normalized, k, nseed, xbin, ybin, mbin, title, color, realtime):
+        """The text of the [muplane] section save_chistogram writes for the histogram of mu
+        (fill_chist) with this metadata and colour rule argument."""
+        import tempfile
+        z = _cplx_array(mu)
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "muplane.dat")
+            self.L.ref_save_chistogram(len(z) // 2, z, int(normalized), np.array([k.real, k.imag]), nseed, xbin,
+                                       ybin, mbin, title.encode(), color.encode(), realtime, fname.encode())
+            with open(fname) as f:
+                return f.read()
 
     def chistogram(self, mu, xbin, ybin, mbin):
         """fill_chist of the complex values mu into a fresh xbin x ybin histogram with an

@@ -22,6 +22,7 @@
 #include "scattering_model_util.h"
 #include "chistogram_type.h"
 #include "chistogram_util.h"
+#include "color_rule_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -279,6 +280,41 @@ void ref_eigvals(int d, int n, int mtype, int np, const double* p, int shape, do
     eigvals(n, a, (dcomplex*)mu);
     free(a);
     drop_medium(&med);
+}
+
+/* eigvals of the normalized MS matrix N(k) = i - G(k)/I(k,0)
+ * (build_normalized_matrix, ms_matrix_util.c:50), the mu-plane task's
+ * mtype=normalized */
+void ref_eigvals_normalized(int d, int n, int mtype, int np, const double* p, int shape, double ratio,
+                            unsigned long seed, const double* k, double* mu) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, seed);
+    dcomplex* a = (dcomplex*)malloc(sizeof(dcomplex) * (size_t)n * n);
+    build_normalized_matrix(&med, k[0] + I * k[1], a);
+    eigvals(n, a, (dcomplex*)mu);
+    free(a);
+    drop_medium(&med);
+}
+
+/* save_chistogram (chistogram_util.c:414): the [muplane] section of a histogram
+ * filled by fill_chist from the nz values z, with the given metadata and colour
+ * rule argument (parse_colorrule's "<name> <seq|div> <ctr> [rev]"), appended to
+ * fname */
+void ref_save_chistogram(int nz, const double* z, int normalized_type, const double* k, int nseed, int xbin,
+                         int ybin, int mbin, const char* title, const char* color, double realtime,
+                         const char* fname) {
+    Chistogram ch;
+    memset(&ch, 0, sizeof(ch));
+    init_chistogram(&ch, normalized_type ? normalized : msmatrix, k[0] + I * k[1], nseed, xbin, ybin, mbin, title);
+    char arg[128];
+    strncpy(arg, color, sizeof(arg) - 1);
+    arg[sizeof(arg) - 1] = '\0';
+    parse_colorrule(ch.colrule, arg);
+    fill_chist(&ch, nz, (dcomplex*)z);
+    ch.realtime = realtime;
+    save_chistogram(&ch, fname);
+    free(ch.colrule->data);
+    del_chistogram(&ch);
 }
 
 /* fill_chist (chistogram_util.c:253) of the nz complex values z into a fresh

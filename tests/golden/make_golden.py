@@ -175,14 +175,28 @@ def reference_runs():
 
 def chistogram_cases(r):
     """mu-plane histograms (run_chistogram_omp, ms_core.c:173-232): the
-    eigenvalues of M(k) of seeds 1..nseed binned by the reference's fill_chist."""
+    eigenvalues of M(k) (or of the normalized N(k), build_normalized_matrix) of
+    seeds 1..nseed binned by the reference's fill_chist; the [muplane] section
+    its save_chistogram writes for each; and the eigenvalues of N(k) of one
+    realisation."""
     out = []
-    for d, n, nseed, k, xbin, ybin, mbin in ((3, 60, 3, 1.3, 16, 12, 10), (2, 50, 2, 2.0, 12, 9, 8)):
-        mus = [r.eigvals(d, n, s, k) for s in range(1, nseed + 1)]
+    for mtype, d, n, nseed, k, xbin, ybin, mbin, color in (
+            ("msmatrix", 3, 60, 3, 1.3, 16, 12, 10, "magma seq 3"),
+            ("msmatrix", 2, 50, 2, 2.0, 12, 9, 8, "viridis div 2.5 rev"),
+            ("normalized", 3, 50, 2, 1.1, 10, 8, 6, "magma seq 3")):
+        eig = r.eigvals_normalized if mtype == "normalized" else r.eigvals
+        mus = [eig(d, n, s, k) for s in range(1, nseed + 1)]
         data, mdata, info = r.chistogram(np.concatenate(mus), xbin, ybin, mbin)
-        out.append({"kind": "chistogram", "d": d, "n": n, "nseed": nseed, "k": [k, 0.0], "xbin": xbin,
-                    "ybin": ybin, "mbin": mbin, "mu": [_cl(m) for m in mus], "data": data.ravel().tolist(),
-                    "mdata": mdata.tolist(), "info": info})
+        title = f"{mtype} d={d}"
+        text = r.save_chistogram(np.concatenate(mus), mtype == "normalized", complex(k), nseed, xbin, ybin, mbin,
+                                 title, color, 2.5)
+        out.append({"kind": "chistogram", "mtype": mtype, "d": d, "n": n, "nseed": nseed, "k": [k, 0.0],
+                    "xbin": xbin, "ybin": ybin, "mbin": mbin, "mu": [_cl(m) for m in mus],
+                    "data": data.ravel().tolist(), "mdata": [float(v) for v in mdata], "info": info,
+                    "muplane": {"title": title, "color": color, "realtime": 2.5, "text": text}})
+    d, n, seed, k = 3, 60, 1, complex(1.2, -0.05)
+    out.append({"kind": "eigvals", "mtype": "normalized", "d": d, "n": n, "seed": seed, "k": [k.real, k.imag],
+                "mu": _cl(r.eigvals_normalized(d, n, seed, k))})
     return out
 
 
@@ -193,7 +207,8 @@ if __name__ == "__main__":
         path = os.path.join(HERE, "reference_runs.json")
         with open(path) as f:
             runs = json.load(f)
-        runs["cases"] = [c for c in runs["cases"] if c["kind"] != "chistogram"] + chistogram_cases(Reference())
+        runs["cases"] = [c for c in runs["cases"] if c["kind"] != "chistogram" and c.get("mtype") != "normalized"] \
+            + chistogram_cases(Reference())
         with open(path, "w") as f:
             json.dump(runs, f, indent=0)
         sys.exit(0)

@@ -15,17 +15,18 @@ def _cases(ref_runs):
 def test_chistogram_matches_reference(ref_runs):
     from msmodel_gb300 import chistogram
     cases = _cases(ref_runs)
-    assert len(cases) == 2
+    assert len(cases) == 3 and {c["mtype"] for c in cases} == {"msmatrix", "normalized"}
     for c in cases:
         mus = [cplx(m) for m in c["mu"]]
         h = chistogram(mus, c["xbin"], c["ybin"], c["mbin"])
         info = c["info"]
         assert np.array_equal(h["data"].ravel(), np.asarray(c["data"]))
-        assert np.allclose(h["mdata"], c["mdata"], rtol=1e-12, atol=0)
+        assert np.array_equal(h["mdata"], np.asarray(c["mdata"]))  # bits: the C library's log and exp
         assert h["dom"] == [info["xmin"], info["xmax"], info["ymin"], info["ymax"]]
         assert h["mrange"] == [info["mmin"], info["mmax"]]
-        assert abs(h["avg"] - complex(info["avg_re"], info["avg_im"])) < 1e-14
-        assert abs(h["sigma"] - complex(info["sigma_re"], info["sigma_im"])) < 1e-14
+        # the moments summed in the reference's order: its bits
+        assert h["avg"] == complex(info["avg_re"], info["avg_im"])
+        assert h["sigma"] == complex(info["sigma_re"], info["sigma_im"])
         assert h["lost"] == info["lost"]
 
 
@@ -39,3 +40,19 @@ def test_chistogram_domain_and_lost():
     assert h["data"][0, 2] == 1
     np.testing.assert_allclose(np.sum(h["mdata"] * 0.1 * np.exp(np.log(10.0) / 2 * np.arange(3)) * np.log(10.0) / 2),
                                1.0, rtol=1e-12)
+
+
+def test_muplane_section_matches_reference(ref_runs, tmp_path):
+    """The [muplane] section (save_chistogram, chistogram_util.c:414-440) of each
+    histogram, byte for byte the text the reference's own writer produced for
+    the same eigenvalues, metadata and colour rule."""
+    from msmodel_gb300 import chistogram
+    from msmodel_gb300.datio import save_muplane
+    for i, c in enumerate(_cases(ref_runs)):
+        h = chistogram([cplx(m) for m in c["mu"]], c["xbin"], c["ybin"], c["mbin"])
+        mp = c["muplane"]
+        name, ctype, ctr, *rev = mp["color"].split()
+        f = tmp_path / f"mu{i}.dat"
+        save_muplane(str(f), h, complex(*c["k"]), c["nseed"], c["mtype"], mp["title"],
+                     (name, ctype, float(ctr), bool(rev)), mp["realtime"])
+        assert f.read_text() == mp["text"]

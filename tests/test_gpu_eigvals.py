@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_eigvals_reference_runs(ms, ref_runs):
-    cases = [c for c in ref_runs["cases"] if c["kind"] == "eigvals"]
+    cases = [c for c in ref_runs["cases"] if c["kind"] == "eigvals" and c.get("mtype", "msmatrix") == "msmatrix"]
     assert len(cases) == 2
     media = [ms.Medium(c["d"], c["n"], seed=c["seed"]) for c in cases]
     ks = [complex(*c["k"]) for c in cases]
@@ -48,6 +48,18 @@ def test_eigvals_larger_against_oracle_matrix(ms, oracle):
         _match_sets(mu, want, 1e-10)
 
 
+def test_eigvals_normalized_reference_run(ms, ref_runs):
+    """mtype=normalized: the eigenvalues of N(k) = i - G(k)/I(k,0)
+    (build_normalized_matrix) against the reference's zgeev of its own N(k)."""
+    cases = [c for c in ref_runs["cases"] if c["kind"] == "eigvals" and c.get("mtype") == "normalized"]
+    assert len(cases) == 1
+    c = cases[0]
+    med = ms.Medium(c["d"], c["n"], seed=c["seed"])
+    mus, st = ms.eigvals_batch([med], [complex(*c["k"])], item_med=[0], mtype="normalized")
+    assert np.all(st == 0)
+    _match_sets(mus[0], cplx(c["mu"]), 1e-10)
+
+
 def test_eigvals_tiny_matrices(ms, oracle):
     """n = 1 (the QR returns the diagonal), 2 (no Householder step) and 3 (one),
     against LAPACK on the oracle's M(k)."""
@@ -67,7 +79,7 @@ def test_run_chistogram_matches_reference(ms, ref_runs):
     at most two counts differ, the moments agree to 1e-10."""
     for c in [c for c in ref_runs["cases"] if c["kind"] == "chistogram"]:
         media = [ms.Medium(c["d"], c["n"], seed=s) for s in range(1, c["nseed"] + 1)]
-        h = ms.run_chistogram(media, complex(*c["k"]), c["xbin"], c["ybin"], c["mbin"])
+        h = ms.run_chistogram(media, complex(*c["k"]), c["xbin"], c["ybin"], c["mbin"], mtype=c["mtype"])
         assert np.all(h["status"] == 0)
         assert np.abs(h["data"].ravel() - np.asarray(c["data"])).sum() <= 2
         info = c["info"]
