@@ -254,11 +254,13 @@ int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const in
  * ms_core.c:173-232): MSGPU_MTYPE_MSMATRIX, M(k), as msgpu_eigvals_batch; or
  * MSGPU_MTYPE_NORMALIZED, N(k) = i - G(k)/I(k,0) with I(k,0) = -Im G(k, 0)
  * (build_normalized_matrix, ms_matrix_util.c:50), independent of the
- * scattering model. */
+ * scattering model.  trg2 (may be NULL) receives per item Tr[G^+ G]/N of the
+ * matrix, 2 sum_{i<j} |A_ij|^2 / n (tracegtwo, ms_matrix_util.c:167), which the
+ * Im mu histogram task uses for its expected variance. */
 #define MSGPU_MTYPE_MSMATRIX 0
 #define MSGPU_MTYPE_NORMALIZED 1
 int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium* media, int nitem, const int* item_med,
-                              const double* ks, double* mu, int* status);
+                              const double* ks, double* mu, int* status, double* trg2);
 
 /* Launch choices (autotuning).  Per (kind, requested precision, size bucket
  * of the job's largest n: (2^(b-1), 2^b]) the engine that runs and the

@@ -91,7 +91,8 @@ def lib():
     L.msgpu_find_roots_muller_batch.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), _dp, C.c_int, _dp, C.c_int,
                                                 C.c_double, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
     L.msgpu_eigvals_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip]
-    L.msgpu_eigvals_batch_mtype.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip]
+    L.msgpu_eigvals_batch_mtype.argtypes = [C.c_int, C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip,
+                                            C.c_void_p]
     L.msgpu_tune_set.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.msgpu_tune_get.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.msgpu_autotune.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
@@ -488,45 +489,89 @@ def inverse_iteration_batch(media, ks, item_med=None, want_vecs=True):
 MTYPES = {"msmatrix": 0, "normalized": 1}
 
 
-def eigvals_batch(media, ks, item_med=None, mtype="msmatrix"):
+def eigvals_batch(media, ks, item_med=None, mtype="msmatrix", want_trg2=False):
     """The n eigenvalues per item (eigvals, ms_matrix_util.c:147) of M(k), or
     with mtype "normalized" of N(k) = i - G(k)/I(k,0) (build_normalized_matrix,
-    ms_matrix_util.c:50): (list of arrays, status)."""
+    ms_matrix_util.c:50): (list of arrays, status), and with want_trg2 also
+    each item's Tr[G^+ G]/N (tracegtwo, ms_matrix_util.c:167)."""
     media = [media] if isinstance(media, Medium) else list(media)
     kk, nitem, im = _items(media, ks, item_med)
     mu = np.zeros(2 * sum(media[i].n for i in im))
     st = np.zeros(nitem, dtype=np.int32)
-    _check(lib().msgpu_eigvals_batch_mtype(MTYPES[mtype], len(media), _media_array(media), nitem, im, kk, mu, st),
-           "eigvals_batch")
+    trg = np.zeros(nitem) if want_trg2 else None
+    _check(lib().msgpu_eigvals_batch_mtype(MTYPES[mtype], len(media), _media_array(media), nitem, im, kk, mu, st,
+                                           trg.ctypes.data if want_trg2 else None), "eigvals_batch")
     mu = mu.view(np.complex128)
     out, off = [], 0
     for i in im:
         out.append(mu[off:off + media[i].n].copy())
         off += media[i].n
-    return out, st
+    return (out, st, trg) if want_trg2 else (out, st)
 
 
 def imag_mu_histogram(mus, nbin, xmin, xmax):
     """Histogram of Im mu on log-spaced bins over [xmin, xmax] (0 < xmin), as
     run_imag_mu_histogram_omp builds it (imag_mu_histogram_util.c:108-153):
     bin floor(nbin (ln Im mu - ln xmin) / ln(xmax/xmin)), samples outside the
-    range lost, then normalised to unit integral (each bin divided by its
-    width, total * x_centre * ln(xmax/xmin)/nbin).  Returns (density, bin
-    centres, lost count)."""
+    range lost, then normalised to unit integral, bin i divided by x_i fac with
+    fac = total ln(xmax/xmin)/nbin and x_i = xmin exp(ln(xmax/xmin)(i + 1/2)/nbin)
+    the bin's centre; the C library's log and exp, in the reference's order of
+    operations.  Returns (density, bin centres, lost count)."""
     x = np.concatenate([np.asarray(m).imag for m in mus])
     counts = np.zeros(nbin)
-    lost = 0
-    lo, hi = np.log(xmin), np.log(xmax)
+    lo, hi = _c_log(xmin), _c_log(xmax)
     with np.errstate(divide="ignore", invalid="ignore"):
-        idx = np.floor(nbin * (np.log(x) - lo) / (hi - lo))
+        idx = np.floor(nbin * (np.array([_c_log(v) for v in x]) - lo) / (hi - lo))
     ok = np.isfinite(idx) & (idx >= 0) & (idx < nbin)
     np.add.at(counts, idx[ok].astype(int), 1.0)
     lost = int(x.size - ok.sum())
-    centres = xmin * np.exp(np.log(xmax / xmin) * (np.arange(nbin) + 0.5) / nbin)
-    total = counts.sum()
-    dens = counts / (centres * total * np.log(xmax / xmin) / nbin) if total else counts
+    lw = _c_log(xmax / xmin)
+    centres = np.array([xmin * _c_exp(lw * (i + 0.5) / nbin) for i in range(nbin)])
+    total = float(np.cumsum(counts)[-1]) if nbin else 0.0
+    fac = total * lw / nbin
+    dens = counts / (centres * fac) if total else counts
     return dens, centres, lost
 
+
+def imag_mu_task(mus, nbin, avgx, trg2):
+    """The arithmetic of run_imag_mu_histogram_omp (ms_core.c:237-288) from the
+    eigenvalues of the realisations of seeds 1, 2, ... in order (mus[s-1]), the
+    exact mean avgx = Re I(k, 0) of Im mu and each realisation's Tr[G^+ G]/N
+    (trg2): the range from seed 1 (setup_domain_ihist: the smallest positive and
+    the largest Im mu, halved and doubled), the histogram (imag_mu_histogram),
+    the true variance sum (Im mu - avgx)^2 / (nseed n) and the expected one
+    sum Tr[G^+ G]/(4 N) / nseed, summed in order as one thread of the reference
+    does.  Returns dict(data, centres, xmin, xmax, avgx, varx_true, varx_expc,
+    lost)."""
+    y0 = np.asarray(mus[0]).imag
+    xmin = xmax = float(y0[0])
+    for v in y0[1:]:
+        v = float(v)
+        if v < xmin and v > 0.0:
+            xmin = v
+        if v > xmax:
+            xmax = v
+    xmin, xmax = xmin / 2.0, 2.0 * xmax
+    data, centres, lost = imag_mu_histogram(mus, nbin, xmin, xmax)
+    y = np.concatenate([np.asarray(m).imag for m in mus])
+    varx_true = float(np.cumsum((y - avgx) * (y - avgx))[-1]) / (len(mus) * len(y0))
+    varx_expc = float(np.cumsum(0.25 * np.asarray(trg2, dtype=np.float64))[-1]) / len(mus)
+    return {"data": data, "centres": centres, "xmin": xmin, "xmax": xmax, "avgx": float(avgx),
+            "varx_true": varx_true, "varx_expc": varx_expc, "lost": lost}
+
+
+def run_imag_mu_histogram(media, k, nbin):
+    """run_imag_mu_histogram_omp (ms_core.c:237-288) for the realisations of
+    media (seeds 1, 2, ... in order) at real k: the eigenvalues and each
+    Tr[G^+ G]/N on the GPU (eigvals_batch), I(k, 0) by the GPU's Green function,
+    the rest by imag_mu_task.  Adds "status"."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    mus, st, trg = eigvals_batch(media, np.full(len(media), complex(k)), np.arange(len(media), dtype=np.int32),
+                                 want_trg2=True)
+    avgx = complex(np.asarray(free_green_imag(media[0].d, [complex(k)], [0.0])).reshape(-1)[0]).real
+    out = imag_mu_task(mus, nbin, avgx, trg)
+    out["status"] = st
+    return out
 
 def _c_round(v):
     """C's round(): halves away from zero (numpy rounds them to even)."""

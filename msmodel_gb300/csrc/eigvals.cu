@@ -53,6 +53,7 @@ struct EigParams {
     zc* work;                // one nmax x nmax slot per CTA
     size_t slot;
     int normalized;          // N(k) = i - G(k)/I(k,0) in place of M(k)
+    double* trg2;            // per item Tr[G^+ G]/N of the matrix (tracegtwo), or nullptr
 };
 
 __device__ __forceinline__ double dlapy3(double x, double y, double z) {
@@ -367,6 +368,14 @@ __global__ void __launch_bounds__(NT, 2) k_eigvals(EigParams P) {
             }
             __syncthreads();
         }
+        if (P.trg2) {
+            // tracegtwo (ms_matrix_util.c:167): 2 sum_{i<j} |A_ij|^2 / n, the matrix symmetric
+            double t = 0.0, z1 = 0.0, z2 = 0.0;
+            for (size_t e = threadIdx.x; e < (size_t)n * n; e += NT)
+                if (e % n < e / n) t += zabs2(A[e]);
+            block_sum3(t, z1, z2, s);
+            if (threadIdx.x == 0) P.trg2[it] = 2.0 * t / n;
+        }
         hessenberg(A, n, s);
         const int info = hqr_cta(A, n, P.mu + P.item_out[it], q);
         if (threadIdx.x == 0) P.status[it] = info > 0 ? MSGPU_S_NOCONV : 0;
@@ -381,7 +390,8 @@ std::mutex g_eig_mu;
 }
 
 extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium* media, int nitem,
-                                         const int* item_med, const double* ks, double* mu, int* status) {
+                                         const int* item_med, const double* ks, double* mu, int* status,
+                                         double* trg2) {
     using namespace msg;
     if ((mtype != MSGPU_MTYPE_MSMATRIX && mtype != MSGPU_MTYPE_NORMALIZED) || nmed < 1 || !media || nitem < 1 || !ks ||
         !mu)
@@ -426,17 +436,19 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
     double *dpos = nullptr, *dks = nullptr;
     zc *dmu = nullptr, *dwork = nullptr;
     int *dn = nullptr, *dd = nullptr, *dst = nullptr;
+    double* dtrg = nullptr;
     size_t *dposo = nullptr, *douto = nullptr;
     msgpu_model* dmodel = nullptr;
     auto cleanup = [&]() {
         cudaFree(dpos); cudaFree(dks); cudaFree(dmu); cudaFree(dwork); cudaFree(dn); cudaFree(dd);
-        cudaFree(dst); cudaFree(dposo); cudaFree(douto); cudaFree(dmodel);
+        cudaFree(dst); cudaFree(dposo); cudaFree(douto); cudaFree(dmodel); cudaFree(dtrg);
     };
     if (cudaMalloc(&dpos, sizeof(double) * npos) || cudaMalloc(&dks, sizeof(double) * 2 * nitem) ||
         cudaMalloc(&dmu, sizeof(zc) * nout) || cudaMalloc(&dwork, sizeof(zc) * slot * grid) ||
         cudaMalloc(&dn, sizeof(int) * nitem) || cudaMalloc(&dd, sizeof(int) * nitem) ||
         cudaMalloc(&dst, sizeof(int) * nitem) || cudaMalloc(&dposo, sizeof(size_t) * nitem) ||
-        cudaMalloc(&douto, sizeof(size_t) * nitem) || cudaMalloc(&dmodel, sizeof(msgpu_model) * nitem)) {
+        cudaMalloc(&douto, sizeof(size_t) * nitem) || cudaMalloc(&dmodel, sizeof(msgpu_model) * nitem) ||
+        (trg2 && cudaMalloc(&dtrg, sizeof(double) * nitem))) {
         cleanup();
         return MSGPU_E_CUDA;
     }
@@ -456,13 +468,14 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
         return MSGPU_E_CUDA;
     }
     EigParams P{nitem, dn, dd, dposo, dmodel, dpos, dks, douto, dmu, dst, dwork, slot,
-                mtype == MSGPU_MTYPE_NORMALIZED};
+                mtype == MSGPU_MTYPE_NORMALIZED, dtrg};
     k_eigvals<<<grid, NT, sizeof(LuSmem)>>>(P);
     count_launches(1);
     std::vector<int> hst(nitem);
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
         cudaMemcpy(mu, dmu, sizeof(zc) * nout, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(hst.data(), dst, sizeof(int) * nitem, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaMemcpy(hst.data(), dst, sizeof(int) * nitem, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (trg2 && cudaMemcpy(trg2, dtrg, sizeof(double) * nitem, cudaMemcpyDeviceToHost) != cudaSuccess)) {
         cleanup();
         return MSGPU_E_CUDA;
     }
@@ -474,5 +487,5 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
 
 extern "C" int msgpu_eigvals_batch(int nmed, const msgpu_medium* media, int nitem, const int* item_med,
                                    const double* ks, double* mu, int* status) {
-    return msgpu_eigvals_batch_mtype(MSGPU_MTYPE_MSMATRIX, nmed, media, nitem, item_med, ks, mu, status);
+    return msgpu_eigvals_batch_mtype(MSGPU_MTYPE_MSMATRIX, nmed, media, nitem, item_med, ks, mu, status, nullptr);
 }

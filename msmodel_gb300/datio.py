@@ -15,6 +15,10 @@ appends the section it names with the same keys, order and number formats:
                      eigenstate_util.c:202-213)
   [muplane]          save_chistogram       src/core/chistogram_util.c:414-440
                      (domain: save_domain; color line: save_colorrule)
+  [imag_mu]          save_ihist            src/core/imag_mu_histogram_util.c:195-213
+  [wavefunction]     save_wfun             src/core/wave_function_util.c:228-245
+                     (k and source: save_iwave, incident_wave_util.c:101;
+                     function=/density=: save_real_data, real_vector_util.c:166)
   data= line         save_cdata            src/core/complex_data_util.c:21-28
 
 `parse_cdata` reads a data= line back (parse_complex_data,
@@ -26,7 +30,7 @@ import math
 import numpy as np
 
 __all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
-           "save_random_function", "save_eigenstate_list", "save_muplane"]
+           "save_random_function", "save_eigenstate_list", "save_muplane", "save_imag_mu", "save_wavefunction"]
 
 MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
@@ -138,4 +142,39 @@ def save_muplane(fname, hist, k, nseed, mtype="msmatrix", title="", color=("magm
     mdata = np.asarray(hist["mdata"])
     text += "mbin=%d\nmrange=%.16g:%.16g\n" % (mdata.size, hist["mrange"][0], hist["mrange"][1])
     text += "mdata=" + "".join(_g16(v) + " " for v in mdata) + "\n\n"
+    _append(fname, text)
+
+
+def _colorrule(key, color):
+    name, ctype, ctr, rev = color
+    return "%s=%s %s %g%s\n" % (key, name, ctype, ctr, " rev" if rev else "")
+
+
+def _real_data(key, values):
+    return key + "=" + "".join(_g16(v) + " " for v in np.asarray(values, dtype=np.float64).reshape(-1)) + "\n"
+
+
+def save_imag_mu(fname, hist, k, nseed, title="", realtime=0.0):
+    """An [imag_mu] section for the Im mu histogram hist (the dict imag_mu_task /
+    run_imag_mu_histogram return) at real k over nseed realisations."""
+    text = "[imag_mu]\ntitle=%s\nk=%g\nnseed=%d\nnbin=%d\n" % (title, k, nseed, len(hist["data"]))
+    text += "xmin=%s\nxmax=%s\navgx=%s\n" % (_g16(hist["xmin"]), _g16(hist["xmax"]), _g16(hist["avgx"]))
+    text += "varx_true=%s\nvarx_expc=%s\nrealtime=%g\n" % (_g16(hist["varx_true"]), _g16(hist["varx_expc"]),
+                                                              realtime)
+    text += "data=" + "".join(_g16(v) + " " for v in hist["data"]) + "\n\n"
+    _append(fname, text)
+
+
+def save_wavefunction(fname, function, density, nx, ny, dom, k, nseed, iseed=1, source="plane", realtime=0.0,
+                      color1=("magma", "seq", 3.0, False), color2=("magma", "seq", 3.0, False)):
+    """A [wavefunction] section: the seed-averaged Re psi (function) and |psi|^2
+    (density) on the nx x ny grid over dom = (xmin, xmax, ymin, ymax), row-major
+    from the top row (wave_function / wave_function_batch return them so), for
+    the incident wave of wave number k ("plane" or "spherical")."""
+    k = complex(k)
+    text = "[wavefunction]\nnseed=%d\niseed=%d\nnx=%d\nny=%d\n" % (nseed, iseed, nx, ny)
+    text += "xrange=%.16g:%.16g\nyrange=%.16g:%.16g\n" % tuple(dom)
+    text += "k=%.16g%+.16gi\nsource=%s\nrealtime=%g\n" % (k.real, k.imag, source, realtime)
+    text += _colorrule("color1", color1) + _colorrule("color2", color2)
+    text += _real_data("function", function) + _real_data("density", density) + "\n"
     _append(fname, text)

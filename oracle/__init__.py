@@ -243,6 +243,10 @@ class Reference:
         L.ref_eigvals.argtypes = med + [_dp, _dp]
         L.ref_chistogram.argtypes = [C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
         L.ref_eigvals_normalized.argtypes = med + [_dp, _dp]
+        L.ref_save_wfun.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_ulong, C.c_double,
+                                    C.c_char_p, C.c_char_p, _dp, _dp, C.c_char_p]
+        L.ref_imag_mu.argtypes = med[:-1] + [C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_double, C.c_char_p,
+                                             _dp, _dp]
         L.ref_save_chistogram.argtypes = [C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.c_char_p, C.c_char_p, C.c_double, C.c_char_p]
         L.ref_inverse_iteration.argtypes = med + [_dp, _dp, _dp]
@@ -318,6 +322,33 @@ class Reference:
                                        ybin, mbin, title.encode(), color.encode(), realtime, fname.encode())
             with open(fname) as f:
                 return f.read()
+
+    def save_wfun(self, nx, ny, dom, k, nseed, iseed, realtime, color1, color2, fun, den, spherical=False):
+        """The text of the [wavefunction] section save_wfun writes for these values."""
+        import tempfile
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "wfun.dat")
+            self.L.ref_save_wfun(nx, ny, np.asarray(dom, dtype=np.float64), np.array([k.real, k.imag]),
+                                 int(spherical), nseed, iseed, realtime, color1.encode(), color2.encode(),
+                                 np.ascontiguousarray(fun, dtype=np.float64),
+                                 np.ascontiguousarray(den, dtype=np.float64), fname.encode())
+            with open(fname) as f:
+                return f.read()
+
+    def imag_mu(self, d, n, k, nseed, nbin, title="", realtime=0.0, model="maximum", params=(), shape="ball",
+                ratio=1.0):
+        """run_imag_mu_histogram_omp on one thread and save_ihist: (text of the [imag_mu]
+        section, data[nbin], info dict)."""
+        import tempfile
+        data, info = np.zeros(nbin), np.zeros(6)
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "imag_mu.dat")
+            self.L.ref_imag_mu(*self._med(d, n, model, params, shape, ratio, 1)[:-1], float(k), nseed, nbin,
+                               title.encode(), realtime, fname.encode(), data, info)
+            with open(fname) as f:
+                text = f.read()
+        keys = ["xmin", "xmax", "avgx", "varx_true", "varx_expc", "lost"]
+        return text, data, dict(zip(keys, info.tolist()))
 
     def chistogram(self, mu, xbin, ybin, mbin):
         """fill_chist of the complex values mu into a fresh xbin x ybin histogram with an

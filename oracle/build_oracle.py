@@ -24,6 +24,8 @@ REF_SOURCES = [
     "common_util.c", "root_finder.c", "domain_util.c", "complex_data_util.c",
     # the mu-plane histogram binning (chistogram_util.c) and what its unit pulls in
     "chistogram_util.c", "color_rule_util.c", "color_data_util.c", "tikz_util.c",
+    # the Im mu histogram and the wave function with their .dat writers
+    "imag_mu_histogram_util.c", "wave_function_util.c", "incident_wave_util.c",
 ]
 
 

@@ -23,6 +23,11 @@
 #include "chistogram_type.h"
 #include "chistogram_util.h"
 #include "color_rule_util.h"
+#include "imag_mu_histogram_type.h"
+#include "imag_mu_histogram_util.h"
+#include "wave_function_type.h"
+#include "wave_function_util.h"
+#include "incident_wave_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -333,4 +338,73 @@ void ref_chistogram(int nz, const double* z, int xbin, int ybin, int mbin, doubl
                           creal(ch.avgz), cimag(ch.avgz), creal(ch.sigmaz), cimag(ch.sigmaz), (double)lost};
     memcpy(info, v, sizeof(v));
     del_chistogram(&ch);
+}
+
+/* save_wfun (wave_function_util.c:228): the [wavefunction] section of an nx x ny
+ * wave function with the given metadata and data, appended to fname */
+void ref_save_wfun(int nx, int ny, const double* dom, const double* k, int spherical_source, int nseed,
+                   unsigned long iseed, double realtime, const char* color1, const char* color2, const double* fun,
+                   const double* den, const char* fname) {
+    WaveFunction w;
+    memset(&w, 0, sizeof(w));
+    Domain dm = {dom[0], dom[1], dom[2], dom[3]};
+    IncidentWave iw;
+    init_iwave(&iw, spherical_source ? spherical : plane, k[0] + I * k[1]);
+    init_wfun(&w, nx, ny, &dm, nseed, iseed, &iw);
+    w.realtime = realtime;
+    char a1[128], a2[128];
+    strncpy(a1, color1, sizeof(a1) - 1);
+    a1[sizeof(a1) - 1] = '\0';
+    strncpy(a2, color2, sizeof(a2) - 1);
+    a2[sizeof(a2) - 1] = '\0';
+    parse_colorrule(w.colrule1, a1);
+    parse_colorrule(w.colrule2, a2);
+    memcpy(w.function, fun, sizeof(double) * (size_t)nx * ny);
+    memcpy(w.density, den, sizeof(double) * (size_t)nx * ny);
+    save_wfun(&w, fname);
+    free(w.colrule1->data);
+    free(w.colrule2->data);
+    del_wfun(&w);
+}
+
+/* run_imag_mu_histogram_omp (ms_core.c:237-288) on one thread, calling the
+ * reference's own steps in its order (setup_domain_ihist, free_green_imag,
+ * build_ms_matrix, eigvals, tracegtwo, append_list_ihist, normalize_ihist), then
+ * save_ihist (imag_mu_histogram_util.c:195) to fname; info = {xmin, xmax, avgx,
+ * varx_true, varx_expc, lost} */
+void ref_imag_mu(int d, int n, int mtype, int np, const double* p, int shape, double ratio, double k, int nseed,
+                 int nbin, const char* title, double realtime, const char* fname, double* data, double* info) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, 1);
+    ImagMuHistogram ih;
+    memset(&ih, 0, sizeof(ih));
+    init_ihist(&ih, nbin, nseed, k, title);
+    setup_domain_ihist(&ih, &med);
+    ih.avgx = creal(free_green_imag(med.d, ih.k, 0.));
+    dcomplex* a = (dcomplex*)calloc((size_t)n * n, sizeof(dcomplex));
+    dcomplex* mu = (dcomplex*)calloc((size_t)n, sizeof(dcomplex));
+    double varx_true = 0., varx_expc = 0.;
+    int lost = 0;
+    for (unsigned long s = 1; s <= (unsigned long)nseed; s++) {
+        fill_medium(&med, s);
+        build_ms_matrix(&med, ih.k, a);
+        eigvals(med.n, a, mu);
+        varx_expc += 0.25 * tracegtwo(med.n, a);
+        for (int i = 0; i < med.n; i++) varx_true += (cimag(mu[i]) - ih.avgx) * (cimag(mu[i]) - ih.avgx);
+        lost += append_list_ihist(&ih, med.n, mu);
+    }
+    ih.varx_true += varx_true;
+    ih.varx_expc += varx_expc;
+    normalize_ihist(&ih);
+    ih.varx_true /= nseed * med.n;
+    ih.varx_expc /= ih.nseed;
+    ih.realtime = realtime;
+    save_ihist(&ih, fname);
+    memcpy(data, ih.data, sizeof(double) * (size_t)nbin);
+    const double v[6] = {ih.xmin, ih.xmax, ih.avgx, ih.varx_true, ih.varx_expc, (double)lost};
+    memcpy(info, v, sizeof(v));
+    free(ih.data);
+    free(a);
+    free(mu);
+    drop_medium(&med);
 }

@@ -177,8 +177,9 @@ def chistogram_cases(r):
     """mu-plane histograms (run_chistogram_omp, ms_core.c:173-232): the
     eigenvalues of M(k) (or of the normalized N(k), build_normalized_matrix) of
     seeds 1..nseed binned by the reference's fill_chist; the [muplane] section
-    its save_chistogram writes for each; and the eigenvalues of N(k) of one
-    realisation."""
+    its save_chistogram writes for each; the eigenvalues of N(k) of one
+    realisation; the Im mu histogram task (run_imag_mu_histogram_omp) with its
+    [imag_mu] section; and a [wavefunction] section (save_wfun)."""
     out = []
     for mtype, d, n, nseed, k, xbin, ybin, mbin, color in (
             ("msmatrix", 3, 60, 3, 1.3, 16, 12, 10, "magma seq 3"),
@@ -197,6 +198,27 @@ def chistogram_cases(r):
     d, n, seed, k = 3, 60, 1, complex(1.2, -0.05)
     out.append({"kind": "eigvals", "mtype": "normalized", "d": d, "n": n, "seed": seed, "k": [k.real, k.imag],
                 "mu": _cl(r.eigvals_normalized(d, n, seed, k))})
+    # the Im mu histogram task on one thread, its [imag_mu] section, the reference's
+    # eigenvalues per seed and Tr[G^+ G]/N of each M(k) (the oracle's matrix)
+    from oracle import Oracle
+    o = Oracle()
+    d, n, k, nseed, nbin = 3, 40, 1.3, 3, 8
+    text, data, info = r.imag_mu(d, n, k, nseed, nbin, "imu", 0.75)
+    trg = []
+    for s in range(1, nseed + 1):
+        m = o.ms_matrix(d, n, o.fill_medium(d, n, s), complex(k))
+        trg.append(float(2.0 * np.sum(np.abs(m[np.triu_indices(n, 1)]) ** 2) / n))
+    out.append({"kind": "imag_mu", "d": d, "n": n, "k": k, "nseed": nseed, "nbin": nbin, "title": "imu",
+                "realtime": 0.75, "text": text, "data": data.tolist(), "info": info,
+                "mu": [_cl(r.eigvals(d, n, s, complex(k))) for s in range(1, nseed + 1)], "trg2_of_m": trg})
+    # the [wavefunction] section save_wfun writes for seeded values
+    rng = np.random.default_rng(5)
+    nx, ny, dom, k = 4, 3, [-2.5, 2.5, -1.25, 1.25], complex(1.1, -0.02)
+    fun, den = rng.standard_normal(nx * ny) * 10, rng.random(nx * ny)
+    out.append({"kind": "wavefunction_file", "nx": nx, "ny": ny, "dom": dom, "k": [k.real, k.imag], "nseed": 3,
+                "iseed": 1, "realtime": 4.5, "color1": "magma seq 3", "color2": "viridis div 2 rev",
+                "function": fun.tolist(), "density": den.tolist(),
+                "text": r.save_wfun(nx, ny, dom, k, 3, 1, 4.5, "magma seq 3", "viridis div 2 rev", fun, den)})
     return out
 
 
@@ -207,8 +229,8 @@ if __name__ == "__main__":
         path = os.path.join(HERE, "reference_runs.json")
         with open(path) as f:
             runs = json.load(f)
-        runs["cases"] = [c for c in runs["cases"] if c["kind"] != "chistogram" and c.get("mtype") != "normalized"] \
-            + chistogram_cases(Reference())
+        runs["cases"] = [c for c in runs["cases"] if c["kind"] not in ("chistogram", "imag_mu", "wavefunction_file")
+                         and c.get("mtype") != "normalized"] + chistogram_cases(Reference())
         with open(path, "w") as f:
             json.dump(runs, f, indent=0)
         sys.exit(0)

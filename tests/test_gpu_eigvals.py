@@ -85,3 +85,22 @@ def test_run_chistogram_matches_reference(ms, ref_runs):
         info = c["info"]
         assert abs(h["avg"] - complex(info["avg_re"], info["avg_im"])) < 1e-10
         assert abs(h["sigma"] - complex(info["sigma_re"], info["sigma_im"])) < 1e-10
+
+
+def test_run_imag_mu_histogram_matches_reference(ms, ref_runs):
+    """run_imag_mu_histogram_omp end to end on the GPU (eigenvalues and
+    Tr[G^+ G]/N by the kernel) against the reference's run: the range, mean and
+    true variance to 1e-12, the expected variance against Tr[G^+ G]/(4N) of M(k)
+    (the reference evaluates it on zgeev's overwritten matrix), and the
+    normalised histogram with at most two counts moved between bins."""
+    c = [c for c in ref_runs["cases"] if c["kind"] == "imag_mu"][0]
+    media = [ms.Medium(c["d"], c["n"], seed=s) for s in range(1, c["nseed"] + 1)]
+    h = ms.run_imag_mu_histogram(media, c["k"], c["nbin"])
+    assert np.all(h["status"] == 0)
+    info = c["info"]
+    for key in ("xmin", "xmax", "avgx", "varx_true"):
+        assert abs(h[key] - info[key]) <= 1e-12 * abs(info[key]), key
+    assert abs(h["varx_expc"] - 0.25 * np.mean(c["trg2_of_m"])) <= 1e-12 * h["varx_expc"]
+    total = c["nseed"] * c["n"] - info["lost"]
+    counts = lambda d: np.asarray(d) * h["centres"] * total * np.log(h["xmax"] / h["xmin"]) / c["nbin"]
+    assert np.abs(np.round(counts(h["data"])) - np.round(counts(c["data"]))).sum() <= 2
