@@ -92,6 +92,10 @@ void msgpu_random_doubles(uint64_t seed, int n, double* out);
 void msgpu_kplane_args(int nx, int ny, double xmin, double xmax, double ymin, double ymax, double* ks);
 /* get_arg_ccut (src/core/complex_cut_util.c:32) for l = 0..3(ns+2)-1 */
 void msgpu_kcut_args(int ns, const double* zmin, const double* zmax, double* ks);
+/* init_logcut's logarithmic mesh (src/core/log_cut_util.c:93-96), k_i = rek +
+ * i imkmin exp(ln(imkmax/imkmin) i/(ns-1)), i = 0..ns-1: the log cut that
+ * run_tracelog_omp evaluates for a [logkcut] task (ms_core.c:734-740) */
+void msgpu_logcut_args(int ns, double rek, double imkmin, double imkmax, double* ks);
 /* set_halton_points (src/core/domain_util.c:180); dom = {xmin,xmax,ymin,ymax} */
 void msgpu_halton_points(const double* dom, int n, double* z);
 

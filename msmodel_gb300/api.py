@@ -57,6 +57,7 @@ def lib():
     L.msgpu_random_doubles.argtypes = [C.c_uint64, C.c_int, _dp]
     L.msgpu_kplane_args.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
     L.msgpu_kcut_args.argtypes = [C.c_int, _dp, _dp, _dp]
+    L.msgpu_logcut_args.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _dp]
     L.msgpu_halton_points.argtypes = [_dp, C.c_int, _dp]
     L.msgpu_eval_special.argtypes = [C.c_int, C.c_int, C.POINTER(_Model), C.c_int, _dp, C.c_void_p, _dp]
     L.msgpu_build_matrix.argtypes = [C.POINTER(_Medium), _dp, C.c_int, _dp]
@@ -232,6 +233,16 @@ def kcut_args(ns, zmin, zmax):
     """k of every sample of a complex cut, get_arg_ccut order (complex_cut_util.c:32)."""
     out = np.zeros(2 * 3 * (ns + 2))
     lib().msgpu_kcut_args(ns, _c2(zmin), _c2(zmax), out)
+    return out.view(np.complex128).copy()
+
+
+def logcut_args(ns, rek, imkmin, imkmax):
+    """k of every sample of a log cut (init_logcut, log_cut_util.c:93-96): the
+    points run_tracelog evaluates for the reference's [logkcut] task."""
+    if ns < 2 or imkmin >= 0 or imkmax >= 0:
+        raise ValueError("logcut_args: ns >= 2 and negative end points (as init_logcut requires)")
+    out = np.zeros(2 * ns)
+    lib().msgpu_logcut_args(ns, float(rek), float(imkmin), float(imkmax), out)
     return out.view(np.complex128).copy()
 
 

@@ -158,6 +158,17 @@ void msgpu_kcut_args(int ns, const double* zmin, const double* zmax, double* ks)
     }
 }
 
+// the logarithmic mesh of init_logcut (src/core/log_cut_util.c:93-96):
+// k_i = rek + i imkmin exp(ln(imkmax/imkmin) i / (ns-1)), the sample accumulating
+// at rek as the mesh approaches the real axis
+void msgpu_logcut_args(int ns, double rek, double imkmin, double imkmax, double* ks) {
+    const double lfac = std::log(imkmax / imkmin);
+    for (int i = 0; i < ns; i++) {
+        ks[2 * i] = rek;
+        ks[2 * i + 1] = imkmin * std::exp((lfac * i) / (ns - 1));
+    }
+}
+
 // set_halton_points (src/core/domain_util.c:170-185), indices 1..n
 void msgpu_halton_points(const double* dom, int n, double* z) {
     for (int i = 0; i < n; i++) {

@@ -9,6 +9,7 @@ appends the section it names with the same keys, order and number formats:
   [kplane]           save_complexmap       src/core/complex_map_util.c:236-249
                      (color line: save_colorrule, color_rule_util.c:276-282)
   [kcut]             save_complexcut       src/core/complex_cut_util.c:106-117
+  [logkcut]          save_logcut           src/core/log_cut_util.c:122-134
   [random_function]  save_random_function  src/core/random_function_util.c:178-193
   [eigenstate_list]  save_eigenstate_list  src/core/eigenstate_list_util.c:296-314
                      (domain: save_domain, domain_util.c:83; states: save_eigenstate,
@@ -30,7 +31,8 @@ import math
 import numpy as np
 
 __all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
-           "save_random_function", "save_eigenstate_list", "save_muplane", "save_imag_mu", "save_wavefunction"]
+           "save_random_function", "save_eigenstate_list", "save_muplane", "save_imag_mu", "save_wavefunction",
+           "save_logcut"]
 
 MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
@@ -93,6 +95,13 @@ def save_complexcut(fname, data, ns, kmin, kmax, title="", realtime=0.0, nseed=1
     kmin, kmax = complex(kmin), complex(kmax)
     text = ("[kcut]\ntitle=%s\nrealtime=%g\nnseed=%d\nsample=%d\nkmin=%.12g%+.12gi\nkmax=%.12g%+.12gi\n"
             % (title, realtime, nseed, ns, kmin.real, kmin.imag, kmax.real, kmax.imag))
+    _append(fname, text + format_cdata(data) + "\n")
+
+
+def save_logcut(fname, data, ns, rek, imkmin, imkmax, title="", realtime=0.0, nseed=1):
+    """A [logkcut] section; data at logcut_args' points (ns values)."""
+    text = ("[logkcut]\ntitle=%s\nrealtime=%g\nnseed=%d\nsample=%d\nrek=%.12g\nimkmin=%.12g\nimkmax=%.12g\n"
+            % (title, realtime, nseed, ns, rek, imkmin, imkmax))
     _append(fname, text + format_cdata(data) + "\n")
 
 

@@ -243,6 +243,8 @@ class Reference:
         L.ref_eigvals.argtypes = med + [_dp, _dp]
         L.ref_chistogram.argtypes = [C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
         L.ref_eigvals_normalized.argtypes = med + [_dp, _dp]
+        L.ref_logcut.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_double,
+                                 _dp, _dp, C.c_char_p]
         L.ref_save_wfun.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_ulong, C.c_double,
                                     C.c_char_p, C.c_char_p, _dp, _dp, C.c_char_p]
         L.ref_imag_mu.argtypes = med[:-1] + [C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_double, C.c_char_p,
@@ -349,6 +351,19 @@ class Reference:
                 text = f.read()
         keys = ["xmin", "xmax", "avgx", "varx_true", "varx_expc", "lost"]
         return text, data, dict(zip(keys, info.tolist()))
+
+    def logcut(self, ns, rek, imkmin, imkmax, data=None, nseed=1, title="", realtime=0.0):
+        """init_logcut's mesh (k[ns]) and, with data, the text of the [logkcut] section
+        save_logcut writes: (k, text or None)."""
+        import tempfile
+        k = np.zeros(2 * ns)
+        d = np.zeros(2 * ns) if data is None else _cplx_array(data)
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "logcut.dat")
+            self.L.ref_logcut(ns, rek, imkmin, imkmax, nseed, title.encode(), realtime, d, k,
+                              fname.encode() if data is not None else None)
+            text = open(fname).read() if data is not None else None
+        return k.view(np.complex128).copy(), text
 
     def chistogram(self, mu, xbin, ybin, mbin):
         """fill_chist of the complex values mu into a fresh xbin x ybin histogram with an

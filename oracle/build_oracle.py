@@ -26,6 +26,8 @@ REF_SOURCES = [
     "chistogram_util.c", "color_rule_util.c", "color_data_util.c", "tikz_util.c",
     # the Im mu histogram and the wave function with their .dat writers
     "imag_mu_histogram_util.c", "wave_function_util.c", "incident_wave_util.c",
+    # the log cut's mesh and writer, and the incomplete gamma function its unit calls
+    "log_cut_util.c", "incomplete_gamma.c", "classical_diffusion_util.c",
 ]
 
 

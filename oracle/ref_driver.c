@@ -28,6 +28,8 @@
 #include "wave_function_type.h"
 #include "wave_function_util.h"
 #include "incident_wave_util.h"
+#include "log_cut_type.h"
+#include "log_cut_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -407,4 +409,20 @@ void ref_imag_mu(int d, int n, int mtype, int np, const double* p, int shape, do
     free(a);
     free(mu);
     drop_medium(&med);
+}
+
+/* init_logcut (log_cut_util.c:72): the mesh k[ns] of a log cut; with fname, the
+ * [logkcut] section save_logcut (:122) writes for the data given */
+void ref_logcut(int ns, double rek, double imkmin, double imkmax, int nseed, const char* title, double realtime,
+                const double* data, double* k, const char* fname) {
+    LogCut lc;
+    memset(&lc, 0, sizeof(lc));
+    init_logcut(&lc, ns, rek, imkmin, imkmax, nseed, title);
+    memcpy(k, lc.k, sizeof(dcomplex) * (size_t)ns);
+    if (fname) {
+        memcpy(lc.data, data, sizeof(dcomplex) * (size_t)ns);
+        lc.realtime = realtime;
+        save_logcut(&lc, fname);
+    }
+    del_logcut(&lc);
 }

@@ -166,6 +166,7 @@ def reference_runs():
     for d, n, seed, k in ((3, 60, 1, 1.2 - 0.05j), (2, 50, 2, 0.8 + 0.0j)):
         add("eigvals", d=d, n=n, seed=seed, k=[k.real, k.imag], mu=_cl(r.eigvals(d, n, seed, k)))
     runs["cases"].extend(chistogram_cases(r))
+    runs["cases"].extend(logcut_cases(r))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
@@ -222,6 +223,19 @@ def chistogram_cases(r):
     return out
 
 
+def logcut_cases(r):
+    """The log cut (init_logcut's mesh, log_cut_util.c:93-96) that run_tracelog_omp
+    evaluates for a [logkcut] task (ms_core.c:734-740): the reference's mesh, its
+    ln det/N there and the [logkcut] section save_logcut writes for them."""
+    d, n, seed, ns, rek, imkmin, imkmax = 3, 64, 1, 24, 2.5, -1e-6, -0.4
+    k, _ = r.logcut(ns, rek, imkmin, imkmax)
+    vals = r.tracelog(d, n, seed, k)
+    _, text = r.logcut(ns, rek, imkmin, imkmax, vals, 1, "log cut", 1.5)
+    return [{"kind": "logcut", "d": d, "n": n, "seed": seed, "ns": ns, "rek": rek, "imkmin": imkmin,
+             "imkmax": imkmax, "k": _cl(k), "values": _cl(vals), "title": "log cut", "realtime": 1.5,
+             "text": text}]
+
+
 if __name__ == "__main__":
     if "--chistogram-only" in sys.argv:
         # add or refresh only the mu-plane histogram cases of an existing reference_runs.json
@@ -229,8 +243,10 @@ if __name__ == "__main__":
         path = os.path.join(HERE, "reference_runs.json")
         with open(path) as f:
             runs = json.load(f)
-        runs["cases"] = [c for c in runs["cases"] if c["kind"] not in ("chistogram", "imag_mu", "wavefunction_file")
-                         and c.get("mtype") != "normalized"] + chistogram_cases(Reference())
+        r = Reference()
+        runs["cases"] = [c for c in runs["cases"] if c["kind"] not in ("chistogram", "imag_mu", "wavefunction_file",
+                                                                       "logcut")
+                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r)
         with open(path, "w") as f:
             json.dump(runs, f, indent=0)
         sys.exit(0)

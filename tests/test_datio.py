@@ -66,3 +66,20 @@ def test_eigenstate_list_section(tmp_path):
     assert "st0_kroot=1.5-0.02i\nst0_mu=1e-12+2e-13i\nst0_eigv=0.6+0i 0+0.8i \n" in text
     assert "st1_kroot=2.25-0.5i\nst1_mu=0-3e-11i\nst1_eigv=1+0i 0+0i \n\n" in text
     assert datio.parse_cdata("data=" + text.split("st0_eigv=")[1].split("\n")[0]).tolist() == [0.6, 0.8j]
+
+
+def test_logcut_mesh_and_section_match_reference(ref_runs, tmp_path):
+    """The log cut: init_logcut's mesh bit for bit (logcut_args, the C library's
+    log and exp) and the [logkcut] section byte for byte what save_logcut wrote
+    for the reference's own ln det values there."""
+    import msmodel_gb300 as ms
+    from helpers import cplx
+    c = [c for c in ref_runs["cases"] if c["kind"] == "logcut"][0]
+    k = ms.logcut_args(c["ns"], c["rek"], c["imkmin"], c["imkmax"])
+    assert np.array_equal(k, cplx(c["k"]))
+    f = tmp_path / "logcut.dat"
+    datio.save_logcut(str(f), cplx(c["values"]), c["ns"], c["rek"], c["imkmin"], c["imkmax"], c["title"],
+                      c["realtime"])
+    assert f.read_text() == c["text"]
+    with pytest.raises(ValueError):
+        ms.logcut_args(10, 2.5, 1e-6, -0.4)

@@ -115,3 +115,17 @@ def test_run_tracelog_seed_average(ms, oracle):
         v, _ = oracle.tracelog_batch(3, 60, pos, ks)
         acc = ((s - 1) * acc + v) / s
     assert np.max(rel(got.real, acc.real)) < 1e-11
+
+
+def test_logcut_matches_reference(ms, ref_runs):
+    """The [logkcut] task (run_tracelog_omp on init_logcut's mesh, ms_core.c:734-740):
+    ln det/N at the log cut's points, approaching the real axis down to
+    Im k = -1e-6, against the reference's run, both engines."""
+    c = [c for c in ref_runs["cases"] if c["kind"] == "logcut"][0]
+    med = ms.Medium(c["d"], c["n"], seed=c["seed"])
+    ks = ms.logcut_args(c["ns"], c["rek"], c["imkmin"], c["imkmax"])
+    want = cplx(c["values"])
+    for precision, tol in (("fp64", 1e-10), ("mixed", 1e-8)):
+        got, st = ms.tracelog_batch([med], ks, precision=precision)
+        assert np.all(st == 0)
+        assert np.max(np.abs(got.real - want.real) / np.abs(want.real)) < tol, precision
