@@ -821,8 +821,12 @@ def main():
     peaks = read_peaks()
     if args.precision == "fp64":
         peak = ms.probe_fp64_tflops()
+        # the FP64 tensor path (warp-level m8n8k4 MMA) measured beside it: the engine
+        # runs on whichever is faster, DFMA on GB300
+        peak_mma = ms.probe_fp64_mma_tflops()
         roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "peak_source": "measured DFMA probe on this GPU (MEASURED_PEAKS.json has no FP64 entry)",
+                "fp64_mma_probe_tflops": peak_mma,
                 "algorithmic": "8/3 N^3 real flops per ln det (complex LU), N=1024: 2.863e9",
                 "traffic": None}
     else:

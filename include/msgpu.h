@@ -76,6 +76,9 @@ int msgpu_sm_count(void);
 uint64_t msgpu_launch_count(void);
 /* measured FP64 FMA throughput of the device in TFLOP/s (roofline denominator of the FP64 path) */
 int msgpu_probe_fp64(double* tflops);
+/* The same for the FP64 tensor path (warp-level mma.sync m8n8k4 f64), the
+ * other candidate roofline of the FP64 engine */
+int msgpu_probe_fp64_mma(double* tflops);
 
 /* Tensor-core self-check: one 128 x 64 x 32 bf16 product D = A B^T (A 128x32,
  * B 64x32, row-major f32 holding small integers) through the engine's tcgen05

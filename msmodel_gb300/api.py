@@ -53,6 +53,7 @@ def lib():
     L.msgpu_last_error.restype = C.c_char_p
     L.msgpu_launch_count.restype = C.c_uint64
     L.msgpu_probe_fp64.argtypes = [C.POINTER(C.c_double)]
+    L.msgpu_probe_fp64_mma.argtypes = [C.POINTER(C.c_double)]
     L.msgpu_fill_medium.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, _dp]
     L.msgpu_random_doubles.argtypes = [C.c_uint64, C.c_int, _dp]
     L.msgpu_kplane_args.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
@@ -121,6 +122,13 @@ def probe_fp64_tflops():
     """Measured FP64 FMA throughput (TFLOP/s) of the current device."""
     v = C.c_double(0.0)
     _check(lib().msgpu_probe_fp64(C.byref(v)), "probe_fp64")
+    return v.value
+
+
+def probe_fp64_mma_tflops():
+    """Measured FP64 tensor-core throughput (warp-level m8n8k4 MMA, TFLOP/s)."""
+    v = C.c_double(0.0)
+    _check(lib().msgpu_probe_fp64_mma(C.byref(v)), "probe_fp64_mma")
     return v.value
 
 

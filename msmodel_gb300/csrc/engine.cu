@@ -200,6 +200,28 @@ __global__ void k_probe_dfma(double* sink, int iters, double a, double b) {
     if (s == 12345.678) sink[blockIdx.x] = s;
 }
 
+// FP64 tensor-core throughput probe: 8 independent accumulators per warp of the
+// warp-level m8n8k4 FP64 MMA (512 flops each), the other candidate of the FP64 path
+__global__ void k_probe_dmma(double* sink, int iters, double a, double b) {
+    double c[8][2];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        c[u][0] = threadIdx.x + u;
+        c[u][1] = 0.5 * u;
+    }
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                         : "+d"(c[u][0]), "+d"(c[u][1])
+                         : "d"(a), "d"(b));
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += c[u][0] + c[u][1];
+    if (s == 12345.678) sink[blockIdx.x] = s;
+}
+
 }  // namespace msg
 
 // ---------------------------------------------------------------------------
@@ -369,6 +391,32 @@ int msgpu_probe_fp64(double* tflops) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    return 0;
+}
+
+int msgpu_probe_fp64_mma(double* tflops) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (int e = init_locked(-1)) return e;
+    double* sink = nullptr;
+    CK(cudaMalloc(&sink, sizeof(double) * 4096));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int blocks = g_sms * 4, threads = 256, iters = 2048;
+    k_probe_dmma<<<blocks, threads>>>(sink, 16, 0.999999, 1e-7);  // warm-up
+    g_launches++;
+    CK(cudaEventRecord(e0));
+    k_probe_dmma<<<blocks, threads>>>(sink, iters, 0.999999, 1e-7);
+    g_launches++;
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    // 512 flops per warp-level MMA, 8 per warp and iteration
+    *tflops = 512.0 * 8.0 * iters * (double)blocks * (threads / 32) / (ms * 1e-3) / 1e12;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(sink);
