@@ -103,3 +103,21 @@ def test_imag_mu_histogram_restates_reference_binning():
     assert abs(np.sum(dens * centres * width) - 1.0) < 1e-14
     counts = dens * centres * 4 * width
     assert np.allclose(counts, [1, 1, 0, 2])  # bin edges 1e-3, 5.6e-3, 3.2e-2, 0.18, 1
+
+
+def test_eigvals_entry_rejects_bad_arguments_without_a_gpu(libpath):
+    """msgpu_eigvals_batch_mtype checks its arguments before it touches a device:
+    an unknown matrix type is MSGPU_E_ARG, a matrix beyond the kernel's limit
+    (n > 4097, the reflector lives in shared memory) MSGPU_E_SIZE."""
+    import msmodel_gb300 as ms
+    from msmodel_gb300 import api
+    L = ms.lib()
+    mu = np.zeros(2 * 4098)
+    st = np.zeros(1, dtype=np.int32)
+    ks = np.array([1.0, 0.0])
+    small = ms.Medium(3, 10, pos=np.zeros(30), seed=1)
+    big = ms.Medium(3, 4098, pos=np.zeros(3 * 4098), seed=1)
+    im = np.zeros(1, dtype=np.int32)
+    assert L.msgpu_eigvals_batch_mtype(7, 1, api._media_array([small]), 1, im, ks, mu, st, None) == -1
+    assert L.msgpu_eigvals_batch_mtype(1, 1, api._media_array([big]), 1, im, ks, mu, st, None) == -4
+    assert L.msgpu_eigvals_batch_mtype(0, 0, api._media_array([small]), 1, im, ks, mu, st, None) == -1
