@@ -129,3 +129,21 @@ def test_logcut_matches_reference(ms, ref_runs):
         got, st = ms.tracelog_batch([med], ks, precision=precision)
         assert np.all(st == 0)
         assert np.max(np.abs(got.real - want.real) / np.abs(want.real)) < tol, precision
+
+
+def test_sizes_at_panel_and_tile_edges(ms, oracle):
+    """ln det and dlogf at n = 1, 2 and either side of the 32-column panel and
+    the 128-row tensor-core tile, both engines, against the oracle: partial
+    panels, partial tiles and the single-element matrix."""
+    ks = np.array([1.3 - 0.1j, 2.6 - 0.02j])
+    for n in (1, 2, 5, 31, 32, 33, 127, 128, 129):
+        med = ms.Medium(3, n, seed=n)
+        want, _ = oracle.tracelog_batch(3, n, med.pos, ks)
+        wantd = oracle.dlogf_batch(3, n, med.pos, ks)
+        for precision, tol, told in (("fp64", 1e-11, 1e-10), ("mixed", 1e-8, 1e-7)):
+            got, st = ms.tracelog_batch([med], ks, precision=precision)
+            assert np.all(st == 0), (n, precision)
+            assert np.max(rel(got.real, want.real)) < tol, (n, precision)
+            gd, sd = ms.dk_log_det_batch([med], ks, precision=precision)
+            assert np.all(sd == 0), (n, precision)
+            assert np.max(np.abs(gd - wantd) / np.abs(wantd)) < told, (n, precision)
