@@ -395,26 +395,28 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
     using namespace msg;
     if ((mtype != MSGPU_MTYPE_MSMATRIX && mtype != MSGPU_MTYPE_NORMALIZED) || nmed < 1 || !media || nitem < 1 || !ks ||
         !mu)
-        return MSGPU_E_ARG;
+        return record_error(MSGPU_E_ARG, "eigvals: bad argument (mtype 0 or 1, nmed >= 1, nitem >= 1, non-null pointers)");
     int nmax = 0;
     size_t npos = 0;
     std::vector<size_t> med_pos(nmed);
     for (int m = 0; m < nmed; ++m) {
-        if (media[m].n < 1 || media[m].d < 1 || !media[m].pos) return MSGPU_E_ARG;
+        if (media[m].n < 1 || media[m].d < 1 || !media[m].pos)
+            return record_error(MSGPU_E_ARG, "eigvals: a medium has n < 1, d < 1 or no positions");
         nmax = std::max(nmax, media[m].n);
         med_pos[m] = npos;
         npos += (size_t)media[m].n * media[m].d;
     }
-    if (nmax > EIG_NMAX) return MSGPU_E_SIZE;
+    if (nmax > EIG_NMAX) return record_error(MSGPU_E_SIZE, "eigvals: n > 4097 (the reflector lives in shared memory)");
     for (int i = 0; i < nitem; ++i)
-        if (item_med && (item_med[i] < 0 || item_med[i] >= nmed)) return MSGPU_E_ARG;
+        if (item_med && (item_med[i] < 0 || item_med[i] >= nmed))
+            return record_error(MSGPU_E_ARG, "eigvals: item_med out of range");
     const int sms = msgpu_sm_count();  // initialises the device and the kernels' attributes
-    if (sms < 1) return MSGPU_E_NODEV;
+    if (sms < 1) return record_error(MSGPU_E_NODEV, "eigvals: no CUDA device");
     std::lock_guard<std::mutex> lk(g_eig_mu);
     // on every call: the attribute belongs to the current device
     if (cudaFuncSetAttribute(k_eigvals, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LuSmem)) !=
         cudaSuccess)
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "eigvals: cudaFuncSetAttribute (shared memory) failed");
     std::vector<int> hn(nitem), hd(nitem);
     std::vector<size_t> hpos(nitem), hout(nitem);
     std::vector<msgpu_model> hmodel(nitem);
@@ -430,7 +432,7 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
     }
     const size_t slot = (size_t)nmax * nmax;
     size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return MSGPU_E_CUDA;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return record_error(MSGPU_E_CUDA, "eigvals: cudaMemGetInfo failed");
     const size_t budget = free_b > ((size_t)4 << 30) ? free_b - ((size_t)4 << 30) : free_b / 2;
     const int grid = (int)std::min<size_t>({(size_t)nitem, (size_t)2 * sms, std::max<size_t>(1, budget / (slot * 16))});
     double *dpos = nullptr, *dks = nullptr;
@@ -450,7 +452,7 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
         cudaMalloc(&douto, sizeof(size_t) * nitem) || cudaMalloc(&dmodel, sizeof(msgpu_model) * nitem) ||
         (trg2 && cudaMalloc(&dtrg, sizeof(double) * nitem))) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "eigvals: device allocation failed");
     }
     bool ok = true;
     for (int m = 0; m < nmed && ok; ++m)
@@ -465,7 +467,7 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
     ok = ok && cudaMemset(dmu, 0, sizeof(zc) * nout) == cudaSuccess;  // unconverged values read 0
     if (!ok) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "eigvals: host-to-device copy failed");
     }
     EigParams P{nitem, dn, dd, dposo, dmodel, dpos, dks, douto, dmu, dst, dwork, slot,
                 mtype == MSGPU_MTYPE_NORMALIZED, dtrg};
@@ -477,7 +479,7 @@ extern "C" int msgpu_eigvals_batch_mtype(int mtype, int nmed, const msgpu_medium
         cudaMemcpy(hst.data(), dst, sizeof(int) * nitem, cudaMemcpyDeviceToHost) != cudaSuccess ||
         (trg2 && cudaMemcpy(trg2, dtrg, sizeof(double) * nitem, cudaMemcpyDeviceToHost) != cudaSuccess)) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "eigvals: kernel launch, execution or device-to-host copy failed");
     }
     if (status)
         for (int i = 0; i < nitem; ++i) status[i] = hst[i];

@@ -352,7 +352,11 @@ extern "C" {
 
 namespace msg {
 void count_launches(int n) { g_launches += n; }
-int record_error(int code, const char* what) { return set_err(code, what); }
+// for entry points outside this file's lock (the allocation-free and eigenvalue entries)
+int record_error(int code, const char* what) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return set_err(code, what);
+}
 }  // namespace msg
 
 extern "C" {

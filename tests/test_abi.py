@@ -120,4 +120,5 @@ def test_eigvals_entry_rejects_bad_arguments_without_a_gpu(libpath):
     im = np.zeros(1, dtype=np.int32)
     assert L.msgpu_eigvals_batch_mtype(7, 1, api._media_array([small]), 1, im, ks, mu, st, None) == -1
     assert L.msgpu_eigvals_batch_mtype(1, 1, api._media_array([big]), 1, im, ks, mu, st, None) == -4
+    assert b"4097" in L.msgpu_last_error()
     assert L.msgpu_eigvals_batch_mtype(0, 0, api._media_array([small]), 1, im, ks, mu, st, None) == -1
