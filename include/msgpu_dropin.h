@@ -64,6 +64,29 @@ typedef struct msgpu_ref_rfun {
     double realtime;
 } msgpu_ref_rfun;
 
+/* reference Chistogram (ComplexHistogram_s), src/core/chistogram_type.h:26-52 */
+typedef struct msgpu_ref_chist {
+    int mtype; /* MatrixType: 0 msmatrix, 1 normalized */
+    int xbin;
+    int ybin;
+    int ntot;
+    void* dom;
+    int dom_ok;
+    msgpu_dcomplex k;
+    int nseed;
+    msgpu_dcomplex avgz;
+    msgpu_dcomplex sigmaz;
+    double* data;
+    void* colrule;
+    double realtime;
+    char title[80];
+    int mbin;
+    double mmin;
+    double mmax;
+    double* mdata;
+    int mrange_ok;
+} msgpu_ref_chist;
+
 /* replaces build_ms_matrix, src/core/ms_matrix_util.c:32 */
 void build_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix);
 /* replaces build_dk_ms_matrix, src/core/ms_matrix_util.c:68 */
@@ -84,6 +107,13 @@ void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread
  * sample in one batched GPU job, bins sorted; the medium is left filled with
  * the last seed, as the reference leaves it */
 void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nthread);
+/* replaces run_chistogram_omp, src/core/ms_core.c:173: the eigenvalues of M(k)
+ * (or N(k), mtype normalized) of seeds 1..nseed in one batched GPU kernel, then
+ * the reference's own fill_chist (chistogram_util.c:253) on them, in seed order;
+ * fill_chist is taken from the program the library is linked into (a weak
+ * reference: a program without it gets an error message and no histogram).  The
+ * medium is left untouched, as the reference's private copies leave it. */
+void run_chistogram_omp(msgpu_ref_medium* med, msgpu_ref_chist* chist, int nthread);
 
 #ifdef __cplusplus
 }

@@ -147,6 +147,51 @@ void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread
     free(media); free(pos); free(ks); free(im); free(out);
 }
 
+/* the reference's binning, resolved in the program the library is linked into */
+extern int fill_chist(msgpu_ref_chist* chist, int nz, msgpu_dcomplex* z) __attribute__((weak));
+
+void run_chistogram_omp(msgpu_ref_medium* med, msgpu_ref_chist* chist, int nthread) {
+    (void)nthread;
+    if (!fill_chist) {
+        printf("[ERROR] run_chistogram_omp: fill_chist is not linked in, no histogram computed.\n");
+        return;
+    }
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int d = med->d, n = med->n, nseed = chist->nseed;
+    msgpu_medium* media = (msgpu_medium*)calloc((size_t)nseed, sizeof(msgpu_medium));
+    double* pos = (double*)malloc(sizeof(double) * (size_t)nseed * n * d);
+    double* ks = (double*)malloc(sizeof(double) * 2 * (size_t)nseed);
+    int* im = (int*)malloc(sizeof(int) * (size_t)nseed);
+    int* st = (int*)calloc((size_t)nseed, sizeof(int));
+    msgpu_dcomplex* mu = (msgpu_dcomplex*)malloc(sizeof(msgpu_dcomplex) * (size_t)nseed * n);
+    msgpu_model mdl = to_model(med->scmodel);
+    for (int s = 0; s < nseed; s++) {
+        double* p = pos + (size_t)s * n * d;
+        int e = msgpu_fill_medium(d, n, med->shape, med->ratio, (uint64_t)(s + 1), p);
+        if (e) fail("run_chistogram_omp: fill_medium", e);
+        media[s].d = d;
+        media[s].n = n;
+        media[s].pos = p;
+        media[s].model = mdl;
+        ks[2 * s] = creal(chist->k);
+        ks[2 * s + 1] = cimag(chist->k);
+        im[s] = s;
+    }
+    int e = msgpu_eigvals_batch_mtype(chist->mtype == 1 ? MSGPU_MTYPE_NORMALIZED : MSGPU_MTYPE_MSMATRIX, nseed,
+                                      media, nseed, im, ks, (double*)mu, st, NULL);
+    if (e) fail("run_chistogram_omp", e);
+    for (int s = 0; s < nseed; s++)
+        if (st[s] & MSGPU_S_NOCONV)  /* eigvals' LAPACK warning, ms_matrix_util.c:158 */
+            printf("[LAPACK] The QR algorithm failed to compute all the eigenvalues (seed %d).\n", s + 1);
+    const int nmu = nseed * n;
+    const int lost = fill_chist(chist, nmu, mu);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    chist->realtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+    printf("[INFO] Lost eigenvalues: %d/%d (%.2f%%)\n", lost, nmu, 100.0 * lost / nmu);
+    free(media); free(pos); free(ks); free(im); free(st); free(mu);
+}
+
 void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nthread) {
     (void)nthread;
     struct timespec t0, t1;

@@ -15,6 +15,14 @@ static msgpu_dcomplex arg_cut(void* self, int l) {
     return ((ns - il) * zmin + (il - 1) * zmax) / (ns - 1) + I * dz * (it - 1);
 }
 
+/* stands in for the reference's fill_chist (chistogram_util.c:253), which the
+ * drop-in run_chistogram_omp calls: prints the eigenvalues it is handed */
+int fill_chist(msgpu_ref_chist* chist, int nz, msgpu_dcomplex* z) {
+    for (int i = 0; i < nz; i++)
+        printf("chist%d %d %.17g %.17g\n", chist->mtype, i, creal(z[i]), cimag(z[i]));
+    return 0;
+}
+
 int main(int argc, char** argv) {
     int d = 3, n = argc > 1 ? atoi(argv[1]) : 80;
     double p[2] = {0.0, 0.0};
@@ -58,6 +66,15 @@ int main(int argc, char** argv) {
     rf.data = (double*)calloc(rf.ntot, sizeof(double));
     run_random_function_omp(&med, &rf, 4);
     for (int l = 0; l < rf.ntot; l++) printf("rfun %d %.17g\n", l, rf.data[l]);
+    /* mu-plane histogram task, seeds 1..2 at k = 1.1, both matrix types */
+    for (int mt = 0; mt < 2; mt++) {
+        msgpu_ref_chist ch = {0};
+        ch.mtype = mt;
+        ch.k = 1.1;
+        ch.nseed = 2;
+        run_chistogram_omp(&med, &ch, 4);
+        printf("chist_realtime %d %.17g\n", mt, ch.realtime);
+    }
     free(a); free(med.pos); free(cd.data); free(rf.data);
     return 0;
 }

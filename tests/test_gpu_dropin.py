@@ -34,6 +34,12 @@ def test_dropin_program(ms, oracle, tmp_path):
             rfun[int(f[1])] = float(f[2])
         elif f[0] == "sigma":
             vals["sigma"] = float(f[1])
+        elif f[0] in ("chist0", "chist1"):
+            vals.setdefault(f[0], []).append(complex(float(f[2]), float(f[3])))
+        elif f[0] == "chist_realtime":
+            vals[f"chist_realtime{f[1]}"] = float(f[2])
+        elif f[0].startswith("["):
+            continue
         else:
             vals[f[0]] = complex(float(f[1]), float(f[2]))
     k = 1.3 - 0.07j
@@ -59,3 +65,20 @@ def test_dropin_program(ms, oracle, tmp_path):
         want = sorted(oracle.total_cross_section(3, n, oracle.fill_medium(3, n, s), kb) for s in (1, 2, 3))
         got = [rfun[3 * i + g] for g in range(3)]
         assert np.max(rel(np.array(got), np.array(want))) < 1e-10
+    # run_chistogram_omp: the eigenvalues of seeds 1 and 2, in seed order, handed to fill_chist;
+    # M(k) and the normalized N(k) = i - G(k)/I(k,0)
+    kc = 1.1 + 0j
+    iz = oracle.free_green_imag(3, kc, 0.0)
+    for mt in (0, 1):
+        mus = vals[f"chist{mt}"]
+        assert len(mus) == 2 * n and vals[f"chist_realtime{mt}"] > 0
+        for s in (1, 2):
+            mm = oracle.ms_matrix(3, n, oracle.fill_medium(3, n, s), kc)
+            if mt == 1:
+                mm = (mm - np.diag(np.diag(mm))) / iz + 1j * np.eye(n)
+            want = list(np.linalg.eigvals(mm))
+            scale = max(abs(w) for w in want)
+            for m in mus[(s - 1) * n:s * n]:
+                j = int(np.argmin([abs(m - w) for w in want]))
+                assert abs(m - want[j]) < 1e-10 * scale
+                want.pop(j)
