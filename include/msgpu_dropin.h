@@ -87,6 +87,21 @@ typedef struct msgpu_ref_chist {
     int mrange_ok;
 } msgpu_ref_chist;
 
+/* reference ImagMuHistogram, src/core/imag_mu_histogram_type.h:16-31 */
+typedef struct msgpu_ref_ihist {
+    int nseed;
+    double k;
+    int nbin;
+    double xmin;
+    double xmax;
+    double* data;
+    double realtime;
+    char title[80];
+    double avgx;
+    double varx_true;
+    double varx_expc;
+} msgpu_ref_ihist;
+
 /* replaces build_ms_matrix, src/core/ms_matrix_util.c:32 */
 void build_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix);
 /* replaces build_dk_ms_matrix, src/core/ms_matrix_util.c:68 */
@@ -114,6 +129,16 @@ void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nt
  * reference: a program without it gets an error message and no histogram).  The
  * medium is left untouched, as the reference's private copies leave it. */
 void run_chistogram_omp(msgpu_ref_medium* med, msgpu_ref_chist* chist, int nthread);
+/* replaces run_imag_mu_histogram_omp, src/core/ms_core.c:225-282: the eigenvalues
+ * and Tr[G^+ G]/N of seeds 1..nseed in one batched GPU kernel; the range from seed
+ * 1's eigenvalues as setup_domain_ihist (imag_mu_histogram_util.c:80) takes it,
+ * without its CPU zgeev, leaving med filled with seed 1 as that function does; the
+ * eigenvalues appended in seed order with the reference's append_list_ihist and
+ * normalised with its normalize_ihist (weak references, resolved from the
+ * program); avgx = Re I(k, 0) by the GPU's Green function.  varx_expc is
+ * Tr[G^+ G]/(4N) of M(k) itself (the reference evaluates it on the matrix zgeev
+ * has overwritten). */
+void run_imag_mu_histogram_omp(msgpu_ref_medium* med, msgpu_ref_ihist* ihist, int nthread);
 
 #ifdef __cplusplus
 }

@@ -553,7 +553,7 @@ def imag_mu_histogram(mus, nbin, xmin, xmax):
 
 
 def imag_mu_task(mus, nbin, avgx, trg2):
-    """The arithmetic of run_imag_mu_histogram_omp (ms_core.c:237-288) from the
+    """The arithmetic of run_imag_mu_histogram_omp (ms_core.c:225-282) from the
     eigenvalues of the realisations of seeds 1, 2, ... in order (mus[s-1]), the
     exact mean avgx = Re I(k, 0) of Im mu and each realisation's Tr[G^+ G]/N
     (trg2): the range from seed 1 (setup_domain_ihist: the smallest positive and
@@ -580,7 +580,7 @@ def imag_mu_task(mus, nbin, avgx, trg2):
 
 
 def run_imag_mu_histogram(media, k, nbin):
-    """run_imag_mu_histogram_omp (ms_core.c:237-288) for the realisations of
+    """run_imag_mu_histogram_omp (ms_core.c:225-282) for the realisations of
     media (seeds 1, 2, ... in order) at real k: the eigenvalues and each
     Tr[G^+ G]/N on the GPU (eigvals_batch), I(k, 0) by the GPU's Green function,
     the rest by imag_mu_task.  Adds "status"."""

@@ -192,6 +192,75 @@ void run_chistogram_omp(msgpu_ref_medium* med, msgpu_ref_chist* chist, int nthre
     free(media); free(pos); free(ks); free(im); free(st); free(mu);
 }
 
+extern int append_list_ihist(msgpu_ref_ihist* ihist, int nz, msgpu_dcomplex* z) __attribute__((weak));
+extern void normalize_ihist(msgpu_ref_ihist* ihist) __attribute__((weak));
+
+void run_imag_mu_histogram_omp(msgpu_ref_medium* med, msgpu_ref_ihist* ih, int nthread) {
+    (void)nthread;
+    if (!append_list_ihist || !normalize_ihist) {
+        printf("[ERROR] run_imag_mu_histogram_omp: the reference's histogram functions are not linked in.\n");
+        return;
+    }
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int d = med->d, n = med->n, nseed = ih->nseed;
+    msgpu_model mdl = to_model(med->scmodel);
+    double kr[2] = {ih->k, 0.0}, r0 = 0.0, iz[2];
+    int e = msgpu_eval_special(2, d, &mdl, 1, kr, &r0, iz);
+    if (e) fail("run_imag_mu_histogram_omp: free_green_imag", e);
+    ih->avgx = iz[0];
+    msgpu_medium* media = (msgpu_medium*)calloc((size_t)nseed, sizeof(msgpu_medium));
+    double* pos = (double*)malloc(sizeof(double) * (size_t)nseed * n * d);
+    double* ks = (double*)malloc(sizeof(double) * 2 * (size_t)nseed);
+    int* im = (int*)malloc(sizeof(int) * (size_t)nseed);
+    int* st = (int*)calloc((size_t)nseed, sizeof(int));
+    double* trg = (double*)malloc(sizeof(double) * (size_t)nseed);
+    msgpu_dcomplex* mu = (msgpu_dcomplex*)malloc(sizeof(msgpu_dcomplex) * (size_t)nseed * n);
+    for (int s = 0; s < nseed; s++) {
+        double* p = pos + (size_t)s * n * d;
+        e = msgpu_fill_medium(d, n, med->shape, med->ratio, (uint64_t)(s + 1), p);
+        if (e) fail("run_imag_mu_histogram_omp: fill_medium", e);
+        media[s].d = d;
+        media[s].n = n;
+        media[s].pos = p;
+        media[s].model = mdl;
+        ks[2 * s] = ih->k;
+        ks[2 * s + 1] = 0.0;
+        im[s] = s;
+    }
+    e = msgpu_eigvals_batch_mtype(MSGPU_MTYPE_MSMATRIX, nseed, media, nseed, im, ks, (double*)mu, st, trg);
+    if (e) fail("run_imag_mu_histogram_omp", e);
+    /* setup_domain_ihist: seed 1's smallest positive and largest Im mu, halved and doubled */
+    double xmin = cimag(mu[0]), xmax = xmin;
+    for (int i = 1; i < n; i++) {
+        const double x = cimag(mu[i]);
+        if (x < xmin && x > 0.0) xmin = x;
+        if (x > xmax) xmax = x;
+    }
+    ih->xmin = xmin / 2.0;
+    ih->xmax = 2.0 * xmax;
+    memcpy(med->pos, pos, sizeof(double) * (size_t)n * d);
+    double varx_true = 0.0, varx_expc = 0.0;
+    int lost = 0;
+    for (int s = 0; s < nseed; s++) {
+        if (st[s] & MSGPU_S_NOCONV)
+            printf("[LAPACK] The QR algorithm failed to compute all the eigenvalues (seed %d).\n", s + 1);
+        msgpu_dcomplex* m = mu + (size_t)s * n;
+        varx_expc += 0.25 * trg[s];
+        for (int i = 0; i < n; i++) varx_true += (cimag(m[i]) - ih->avgx) * (cimag(m[i]) - ih->avgx);
+        lost += append_list_ihist(ih, n, m);
+    }
+    ih->varx_true += varx_true;
+    ih->varx_expc += varx_expc;
+    normalize_ihist(ih);
+    ih->varx_true /= (double)nseed * n;
+    ih->varx_expc /= nseed;
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    ih->realtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+    printf("[INFO] Lost eigenvalues: %d/%d (%.2f%%)\n", lost, nseed * n, 100.0 * lost / (nseed * n));
+    free(media); free(pos); free(ks); free(im); free(st); free(trg); free(mu);
+}
+
 void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nthread) {
     (void)nthread;
     struct timespec t0, t1;

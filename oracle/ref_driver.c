@@ -369,7 +369,7 @@ void ref_save_wfun(int nx, int ny, const double* dom, const double* k, int spher
     del_wfun(&w);
 }
 
-/* run_imag_mu_histogram_omp (ms_core.c:237-288) on one thread, calling the
+/* run_imag_mu_histogram_omp (ms_core.c:225-282) on one thread, calling the
  * reference's own steps in its order (setup_domain_ihist, free_green_imag,
  * build_ms_matrix, eigvals, tracegtwo, append_list_ihist, normalize_ihist), then
  * save_ihist (imag_mu_histogram_util.c:195) to fname; info = {xmin, xmax, avgx,

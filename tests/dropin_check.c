@@ -23,6 +23,20 @@ int fill_chist(msgpu_ref_chist* chist, int nz, msgpu_dcomplex* z) {
     return 0;
 }
 
+/* stand in for the reference's append_list_ihist and normalize_ihist
+ * (imag_mu_histogram_util.c:107,139), which the drop-in run_imag_mu_histogram_omp
+ * calls: print the eigenvalues they are handed and count the normalisations */
+static int n_normalize = 0;
+int append_list_ihist(msgpu_ref_ihist* ih, int nz, msgpu_dcomplex* z) {
+    for (int i = 0; i < nz; i++) printf("ihist %d %.17g %.17g\n", i, creal(z[i]), cimag(z[i]));
+    (void)ih;
+    return 0;
+}
+void normalize_ihist(msgpu_ref_ihist* ih) {
+    (void)ih;
+    n_normalize++;
+}
+
 int main(int argc, char** argv) {
     int d = 3, n = argc > 1 ? atoi(argv[1]) : 80;
     double p[2] = {0.0, 0.0};
@@ -75,6 +89,15 @@ int main(int argc, char** argv) {
         run_chistogram_omp(&med, &ch, 4);
         printf("chist_realtime %d %.17g\n", mt, ch.realtime);
     }
+    /* Im mu histogram task, seeds 1..2 at k = 1.1 */
+    msgpu_ref_ihist ih = {0};
+    ih.k = 1.1;
+    ih.nseed = 2;
+    ih.nbin = 8;
+    run_imag_mu_histogram_omp(&med, &ih, 4);
+    printf("ihist_info %.17g %.17g %.17g %.17g %.17g %d %.17g\n", ih.xmin, ih.xmax, ih.avgx, ih.varx_true,
+           ih.varx_expc, n_normalize, ih.realtime);
+    printf("pos0 %.17g %.17g %.17g\n", med.pos[0], med.pos[1], med.pos[2]);
     free(a); free(med.pos); free(cd.data); free(rf.data);
     return 0;
 }

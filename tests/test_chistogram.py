@@ -65,7 +65,7 @@ def _case(ref_runs, kind):
 
 
 def test_imag_mu_task_matches_reference(ref_runs):
-    """run_imag_mu_histogram_omp's arithmetic (ms_core.c:237-288) on the
+    """run_imag_mu_histogram_omp's arithmetic (ms_core.c:225-282) on the
     reference's eigenvalues: range from seed 1, log-binned density, exact mean
     and true variance, all the reference's bits.  The expected variance is
     Tr[G^+ G]/(4N) of M(k): the reference takes tracegtwo after zgeev has

@@ -36,6 +36,12 @@ def test_dropin_program(ms, oracle, tmp_path):
             vals["sigma"] = float(f[1])
         elif f[0] in ("chist0", "chist1"):
             vals.setdefault(f[0], []).append(complex(float(f[2]), float(f[3])))
+        elif f[0] == "ihist":
+            vals.setdefault("ihist", []).append(complex(float(f[2]), float(f[3])))
+        elif f[0] == "ihist_info":
+            vals["ihist_info"] = [float(x) for x in f[1:]]
+        elif f[0] == "pos0":
+            vals["pos0"] = [float(x) for x in f[1:]]
         elif f[0] == "chist_realtime":
             vals[f"chist_realtime{f[1]}"] = float(f[2])
         elif f[0].startswith("["):
@@ -82,3 +88,29 @@ def test_dropin_program(ms, oracle, tmp_path):
                 j = int(np.argmin([abs(m - w) for w in want]))
                 assert abs(m - want[j]) < 1e-10 * scale
                 want.pop(j)
+    # run_imag_mu_histogram_omp: seeds 1 and 2 of M(1.1) in seed order, the range from seed 1,
+    # avgx = Re I(k, 0), the variances, one normalisation, med left holding seed 1
+    mus = vals["ihist"]
+    assert len(mus) == 2 * n
+    want_all, trg = [], []
+    for s in (1, 2):
+        mm = oracle.ms_matrix(3, n, oracle.fill_medium(3, n, s), kc)
+        want = list(np.linalg.eigvals(mm))
+        scale = max(abs(w) for w in want)
+        got = mus[(s - 1) * n:s * n]
+        for m in got:
+            j = int(np.argmin([abs(m - w) for w in want]))
+            assert abs(m - want[j]) < 1e-10 * scale
+            want.pop(j)
+        want_all.append(got)
+        iu = np.triu_indices(n, 1)
+        trg.append(2.0 * np.sum(np.abs(mm[iu]) ** 2) / n)
+    xmin, xmax, avgx, vt, ve, nnorm, rt = vals["ihist_info"]
+    y1 = np.array(want_all[0]).imag
+    assert xmin == np.min(y1[y1 > 0]) / 2 and xmax == 2 * np.max(y1)
+    assert rel(avgx, iz.real) < 1e-13
+    y = np.concatenate([np.array(g).imag for g in want_all])
+    assert rel(vt, np.mean((y - avgx) ** 2)) < 1e-12
+    assert rel(ve, 0.25 * np.mean(trg)) < 1e-12
+    assert nnorm == 1 and rt > 0
+    assert vals["pos0"] == list(oracle.fill_medium(3, n, 1)[:3])
