@@ -10,7 +10,16 @@ check, with immediate binding at load time, that the relinked program binds
 every hot-path symbol it calls to libmsgpu.so, and that the reference's own
 copies survive only under their cpu_ names.  build_dk_ms_matrix has no caller
 outside ms_matrix_util.c, so it is checked as exported by the library only.
-No GPU is needed: the program prints its usage without touching the device."""
+
+The second test takes the other route, with no renames at all: the reference's
+src/core built unchanged as a shared library (-fPIC keeps GCC's default
+semantic interposition, so calls between its functions go through the PLT) and
+ms_main.c linked against libmsgpu.so ahead of it.  The dynamic linker then binds
+the core's calls of the hot-path functions and of the task drivers defined and
+called inside ms_core.c (run_tracelog_omp, run_random_function_omp,
+run_chistogram_omp, run_imag_mu_histogram_omp) to libmsgpu.so, and libmsgpu's
+weak references to the reference's histogram functions back to the core.
+No GPU is needed: the programs print their usage without touching the device."""
 import concurrent.futures as cf
 import os
 import shutil
@@ -26,6 +35,8 @@ LIB = os.path.join(ROOT, "msmodel_gb300", "libmsgpu.so")
 HOT = ["build_ms_matrix", "build_dk_ms_matrix", "build_plane_wave", "tracelog_lu", "dk_log_det_ms",
        "total_cross_section"]
 CALLED = ["build_ms_matrix", "build_plane_wave", "tracelog_lu", "dk_log_det_ms", "total_cross_section"]
+DRIVERS = ["run_tracelog_omp", "run_random_function_omp", "run_chistogram_omp", "run_imag_mu_histogram_omp"]
+BACK = ["fill_chist", "append_list_ihist", "normalize_ihist"]
 
 
 def _need():
@@ -88,3 +99,59 @@ def test_reference_relinks_against_library(tmp_path):
         lines = [l for l in r.stderr.splitlines() if l.rstrip().endswith(f"symbol `{s}'")]
         assert lines, s
         assert all(os.path.basename(LIB) in l for l in lines), lines
+
+
+def _bindings(exe, cwd):
+    """{(from, to, symbol)} of a start-up with every symbol bound immediately."""
+    env = dict(os.environ, LD_BIND_NOW="1", LD_DEBUG="bindings")
+    r = subprocess.run([exe], capture_output=True, text=True, env=env, cwd=cwd, timeout=120)
+    assert "MSModel" in r.stdout, r.stdout[-500:] + r.stderr[-500:]
+    out = set()
+    for l in r.stderr.splitlines():
+        f = l.split()
+        if "binding" in f and "symbol" in f:
+            i = f.index("binding")
+            out.add((os.path.basename(f[i + 2]), os.path.basename(f[i + 5]), f[-1].strip("`'")))
+    return out
+
+
+def test_reference_core_library_interposed(tmp_path):
+    _need()
+    sys.path.insert(0, ROOT)
+    from oracle.build_oracle import openblas_path
+    ob = openblas_path()
+    if ob is None:
+        pytest.skip("no LAPACK to link the reference against")
+    core = os.path.join(REF, "src", "core")
+    srcs = sorted(os.path.join(core, f) for f in os.listdir(core) if f.endswith(".c"))
+    flags = ["gcc", "-O2", "-w", "-fPIC", "-fms-extensions", "-fopenmp", "-I", core]
+
+    def compile_one(src):
+        obj = str(tmp_path / (os.path.basename(src)[:-2] + ".o"))
+        _run(flags + ["-c", src, "-o", obj])
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    shim = str(tmp_path / "lapack_shim.o")
+    _run(["gcc", "-O1", "-fPIC", "-c", os.path.join(ROOT, "oracle", "lapack_shim.c"), "-o", shim])
+    core_so = str(tmp_path / "libmscore.so")
+    _run(["gcc", "-shared", "-fopenmp"] + objs + [shim, ob, "-Wl,-rpath," + os.path.dirname(ob), "-lm",
+                                                  "-o", core_so])
+    # the two libraries overlap in exactly the names libmsgpu replaces
+    def names(so):
+        return {l.split()[-1] for l in _run(["nm", "-D", "--defined-only", so]).stdout.splitlines() if l.strip()}
+
+    assert names(core_so) & names(LIB) == set(HOT + DRIVERS)
+    exe = str(tmp_path / "msmain")
+    libdir = os.path.dirname(LIB)
+    _run(["gcc", "-O1", "-w", "-fms-extensions", "-fopenmp", "-I", core, os.path.join(REF, "src", "main", "ms_main.c"),
+          "-L", libdir, "-Wl,--no-as-needed", "-lmsgpu", "-Wl,--as-needed", "-L", str(tmp_path), "-lmscore",
+          "-Wl,-rpath," + libdir, "-Wl,-rpath," + str(tmp_path), "-lm", "-o", exe])
+    b = _bindings(exe, str(tmp_path))
+    lib, core_name = os.path.basename(LIB), "libmscore.so"
+    for s in CALLED + ["build_dk_ms_matrix"] + DRIVERS:
+        assert (core_name, lib, s) in b, s
+        assert (core_name, core_name, s) not in b, s
+    for s in BACK:
+        assert (lib, core_name, s) in b, s
