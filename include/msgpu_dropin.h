@@ -10,6 +10,7 @@
 #ifndef MSGPU_DROPIN_H
 #define MSGPU_DROPIN_H
 #include <complex.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -102,6 +103,66 @@ typedef struct msgpu_ref_ihist {
     double varx_expc;
 } msgpu_ref_ihist;
 
+/* reference Domain, src/core/domain_type.h:19-24 */
+typedef struct msgpu_ref_domain {
+    double xmin;
+    double xmax;
+    double ymin;
+    double ymax;
+} msgpu_ref_domain;
+
+/* reference IncidentWave, src/core/incident_wave_type.h:23-31 */
+typedef struct msgpu_ref_iwave {
+    int source; /* IncidentWaveSource: 0 plane, 1 spherical */
+    msgpu_dcomplex k;
+    char desc_ascii[80];
+    char desc_latex[80];
+} msgpu_ref_iwave;
+
+/* reference WaveFunction, src/core/wave_function_type.h:22-41 */
+typedef struct msgpu_ref_wfun {
+    int nseed;
+    uint64_t iseed;
+    msgpu_ref_iwave* iwave;
+    int nx;
+    int ny;
+    msgpu_ref_domain* dom;
+    double dx;
+    double dy;
+    double* function;
+    double* density;
+    void* colrule1;
+    void* colrule2;
+    double realtime;
+} msgpu_ref_wfun;
+
+/* reference Eigenstate, src/core/eigenstate_type.h:23-35 */
+typedef struct msgpu_ref_eigenstate {
+    msgpu_dcomplex kroot;
+    msgpu_dcomplex mu;
+    msgpu_dcomplex* eigv;
+    int isfitted;
+    double* center;
+    double locfac;
+    double ampcst;
+} msgpu_ref_eigenstate;
+
+/* reference EigenstateList, src/core/eigenstate_list_type.h:25-44 */
+typedef struct msgpu_ref_eigls {
+    msgpu_ref_medium* med;
+    uint64_t seed;
+    int method; /* EigenstateMethod: 0 determinant, 1 mineigval, 2 invtraceinv */
+    int ntarget;
+    msgpu_ref_domain* dom;
+    int maxit;
+    double toler;
+    int verb;
+    int nstate;
+    int nfitted;
+    msgpu_ref_eigenstate** eigtab;
+    double realtime;
+} msgpu_ref_eigls;
+
 /* replaces build_ms_matrix, src/core/ms_matrix_util.c:32 */
 void build_ms_matrix(msgpu_ref_medium* med, msgpu_dcomplex k, msgpu_dcomplex* matrix);
 /* replaces build_dk_ms_matrix, src/core/ms_matrix_util.c:68 */
@@ -139,6 +200,30 @@ void run_chistogram_omp(msgpu_ref_medium* med, msgpu_ref_chist* chist, int nthre
  * Tr[G^+ G]/(4N) of M(k) itself (the reference evaluates it on the matrix zgeev
  * has overwritten). */
 void run_imag_mu_histogram_omp(msgpu_ref_medium* med, msgpu_ref_ihist* ihist, int nthread);
+/* replaces run_wave_function_omp, src/core/ms_core.c:596-649, for the plane
+ * incident wave (a spherical source prints an error and leaves the arrays as
+ * they are): the realisations of seeds iseed..iseed+nseed-1 solved and summed
+ * over the nx*ny grid in one batched GPU job (msgpu_wave_function, mixed LU
+ * refined to an FP64 residual); function/density receive the averages added
+ * to their entry values divided by nseed, i.e. (entry + sum)/nseed as the
+ * reference's sum and divide_wfun; med is left holding the last seed. */
+void run_wave_function_omp(msgpu_ref_medium* med, msgpu_ref_wfun* wfun, int nthread);
+/* replace find_eigenstates_serial_1/2/3, src/core/ms_core.c:320-401: the
+ * resonance search on the realisation in eigls->med from the *nroot starting
+ * points kroot, by the determinant (Aberth on dlogf, nexpsup = 4), mineigval or
+ * invtraceinv (Muller) method, every step's function values in one batched
+ * FP64 GPU job (msgpu_solve_aberth_batch, msgpu_find_roots_muller_batch);
+ * kroot and *nroot receive the roots as the reference leaves them; realtime set. */
+void find_eigenstates_serial_1(msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot);
+void find_eigenstates_serial_2(msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot);
+void find_eigenstates_serial_3(msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot);
+/* replaces compute_eigenstates, src/core/ms_core.c:296-313: the eigenvectors
+ * of every root in one batched FP64 GPU job (msgpu_inverse_iteration_batch:
+ * constant unit start, 50 steps, tolerance 1e-10, the only values the
+ * reference passes; others print an error and return), stored through the
+ * reference's own alloc_eigenstate_list and checked with its
+ * check_eigenstate_list (weak references, resolved from the program). */
+void compute_eigenstates(msgpu_ref_eigls* eigls, int nroot, msgpu_dcomplex* kroot, int maxit, double toler, int verb);
 
 #ifdef __cplusplus
 }

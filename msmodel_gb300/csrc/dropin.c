@@ -276,3 +276,142 @@ void run_random_function_omp(msgpu_ref_medium* med, msgpu_ref_rfun* rfun, int nt
     clock_gettime(CLOCK_MONOTONIC, &t1);
     rfun->realtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
 }
+
+static double seconds_since(const struct timespec* t0) {
+    struct timespec t1;
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    return (t1.tv_sec - t0->tv_sec) + 1e-9 * (t1.tv_nsec - t0->tv_nsec);
+}
+
+void run_wave_function_omp(msgpu_ref_medium* med, msgpu_ref_wfun* wf, int nthread) {
+    (void)nthread;
+    if (med->d == 1)  /* the reference's own warning, ms_core.c:597-598 */
+        printf("[WARN] The wavefunction in %dD cannot be computed in the same way as in other dimensions. "
+               "This may lead to strange results...\n", med->d);
+    if (wf->iwave->source != 0) {
+        printf("[ERROR] run_wave_function_omp: libmsgpu builds the plane incident wave only.\n");
+        return;
+    }
+    struct timespec t0;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int d = med->d, n = med->n, ns = wf->nseed, np = wf->nx * wf->ny;
+    if (ns < 1 || np < 1) return;
+    msgpu_model mdl = to_model(med->scmodel);
+    msgpu_medium* media = (msgpu_medium*)calloc((size_t)ns, sizeof(msgpu_medium));
+    double* pos = (double*)malloc(sizeof(double) * (size_t)ns * n * d);
+    double* f = (double*)malloc(sizeof(double) * (size_t)np);
+    double* g = (double*)malloc(sizeof(double) * (size_t)np);
+    for (int s = 0; s < ns; s++) {
+        double* p = pos + (size_t)s * n * d;
+        int e = msgpu_fill_medium(d, n, med->shape, med->ratio, wf->iseed + (uint64_t)s, p);
+        if (e) fail("run_wave_function_omp: fill_medium", e);
+        media[s].d = d;
+        media[s].n = n;
+        media[s].pos = p;
+        media[s].model = mdl;
+    }
+    const double k[2] = {creal(wf->iwave->k), cimag(wf->iwave->k)};
+    const double dom[4] = {wf->dom->xmin, wf->dom->xmax, wf->dom->ymin, wf->dom->ymax};
+    int st = msgpu_wave_function(ns, media, k, wf->nx, wf->ny, dom, f, g, NULL, NULL, MSGPU_MIXED);
+    if (st < 0) fail("run_wave_function_omp", st);
+    if (st & (MSGPU_S_SINGULAR | MSGPU_S_NONFINITE))
+        printf("[WARN] run_wave_function_omp: a singular or non-finite solve reached the averages (status %d).\n", st);
+    for (int l = 0; l < np; l++) {  /* (entry + sum over seeds)/nseed, as the sum and divide_wfun */
+        wf->function[l] = wf->function[l] / ns + f[l];
+        wf->density[l] = wf->density[l] / ns + g[l];
+    }
+    memcpy(med->pos, pos + (size_t)(ns - 1) * n * d, sizeof(double) * (size_t)n * d);
+    wf->realtime = seconds_since(&t0);
+    free(media); free(pos); free(f); free(g);
+}
+
+/* The roots of one realisation: every step's function values in one batched
+ * GPU job; method 0 Aberth (find_eigenstates_serial_1), 1/2 Muller on the
+ * smallest eigenvalue or on 1/tr M^-1 (find_eigenstates_serial_2/3). */
+static void find_roots(int method, msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot) {
+    struct timespec t0;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int nz = *nroot;
+    if (nz < 1) {
+        eigls->realtime = 0.0;
+        return;
+    }
+    msgpu_medium m = to_medium(eigls->med);
+    const double dom[4] = {eigls->dom->xmin, eigls->dom->xmax, eigls->dom->ymin, eigls->dom->ymax};
+    double* z0 = (double*)malloc(sizeof(double) * 2 * (size_t)nz);
+    double* roots = (double*)malloc(sizeof(double) * 2 * (size_t)nz);
+    for (int i = 0; i < nz; i++) {
+        z0[2 * i] = creal(kroot[i]);
+        z0[2 * i + 1] = cimag(kroot[i]);
+    }
+    int nr = 0, e;
+    if (method == 0)  /* nexpsup = 4, as find_eigenstates_serial_1 passes it (ms_core.c:324) */
+        e = msgpu_solve_aberth_batch(1, &m, dom, nz, z0, 4, eigls->maxit, eigls->toler, MSGPU_FP64, roots, &nr, NULL);
+    else
+        e = msgpu_find_roots_muller_batch(method, 1, &m, dom, nz, z0, eigls->maxit, eigls->toler, MSGPU_FP64, roots,
+                                          &nr, NULL);
+    if (e) fail(method == 0 ? "find_eigenstates_serial_1" : method == 1 ? "find_eigenstates_serial_2"
+                                                                        : "find_eigenstates_serial_3", e);
+    for (int i = 0; i < nr; i++) kroot[i] = roots[2 * i] + I * roots[2 * i + 1];
+    *nroot = nr;
+    if (method != 0)  /* the split into duplicates and failures is not kept */
+        printf("[INFO] Found %d/%d valid roots, %d duplicates or failed.\n", nr, eigls->ntarget, nz - nr);
+    eigls->realtime = seconds_since(&t0);
+    free(z0); free(roots);
+}
+
+void find_eigenstates_serial_1(msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot) {
+    find_roots(0, eigls, nroot, kroot);
+}
+
+void find_eigenstates_serial_2(msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot) {
+    find_roots(1, eigls, nroot, kroot);
+}
+
+void find_eigenstates_serial_3(msgpu_ref_eigls* eigls, int* nroot, msgpu_dcomplex* kroot) {
+    find_roots(2, eigls, nroot, kroot);
+}
+
+extern void alloc_eigenstate_list(msgpu_ref_eigls* eigls, int nstate) __attribute__((weak));
+extern void check_eigenstate_list(msgpu_ref_eigls* eigls) __attribute__((weak));
+
+void compute_eigenstates(msgpu_ref_eigls* eigls, int nroot, msgpu_dcomplex* kroot, int maxit, double toler, int verb) {
+    (void)verb;
+    if (!alloc_eigenstate_list || !check_eigenstate_list) {
+        printf("[ERROR] compute_eigenstates: the reference's eigenstate list functions are not linked in.\n");
+        return;
+    }
+    if (maxit != 50 || toler != 1e-10) {
+        printf("[ERROR] compute_eigenstates: libmsgpu runs the inverse iteration with maxit=50, toler=1e-10 only "
+               "(got maxit=%d, toler=%g).\n", maxit, toler);
+        return;
+    }
+    alloc_eigenstate_list(eigls, nroot);
+    const int n = eigls->med->n, ns = eigls->nstate;
+    printf("[EXEC] Computing %d states ... ", ns);
+    fflush(stdout);
+    if (ns > 0) {
+        msgpu_medium m = to_medium(eigls->med);
+        double* ks = (double*)malloc(sizeof(double) * 2 * (size_t)ns);
+        double* lam = (double*)malloc(sizeof(double) * 2 * (size_t)ns);
+        double* vec = (double*)malloc(sizeof(double) * 2 * (size_t)ns * n);
+        int* st = (int*)calloc((size_t)ns, sizeof(int));
+        for (int i = 0; i < ns; i++) {
+            ks[2 * i] = creal(kroot[i]);
+            ks[2 * i + 1] = cimag(kroot[i]);
+        }
+        int e = msgpu_inverse_iteration_batch(1, &m, ns, NULL, ks, lam, vec, st, MSGPU_FP64);
+        if (e) fail("compute_eigenstates", e);
+        for (int i = 0; i < ns; i++) {
+            msgpu_ref_eigenstate* es = eigls->eigtab[i];
+            es->kroot = kroot[i];
+            es->mu = lam[2 * i] + I * lam[2 * i + 1];
+            memcpy(es->eigv, vec + 2 * (size_t)i * n, sizeof(double) * 2 * (size_t)n);
+            if (st[i] & MSGPU_S_SINGULAR)  /* inverse_iteration's warning, ms_matrix_util.c:284 */
+                printf("[LAPACK] Element U(i,i) is exactly zero, the inverse power iteration will fail.\n");
+        }
+        free(ks); free(lam); free(vec); free(st);
+    }
+    printf("Done\n");
+    check_eigenstate_list(eigls);
+}

@@ -114,3 +114,89 @@ def test_dropin_program(ms, oracle, tmp_path):
     assert rel(ve, 0.25 * np.mean(trg)) < 1e-12
     assert nnorm == 1 and rt > 0
     assert vals["pos0"] == list(oracle.fill_medium(3, n, 1)[:3])
+
+
+def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
+    """find_eigenstates_serial_1/2/3 and compute_eigenstates called from C as
+    run_eigenstate_list_serial calls them, against the reference's own runs;
+    run_wave_function_omp against the oracle's seed average."""
+    from msmodel_gb300 import build
+    from helpers import cplx, match_root_sets
+    lib = build.build()
+    exe = tmp_path / "dropin_roots_check"
+    r = subprocess.run(["gcc", "-O1", "-std=gnu11", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "dropin_roots_check.c"), "-o", str(exe), lib,
+                        "-Wl,-rpath," + os.path.dirname(lib), "-lm"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+    def zs(z):
+        return " ".join(f"{float(v.real)!r} {float(v.imag)!r}" for v in z)
+
+    ab = [c for c in ref_runs["cases"] if c["kind"] == "aberth"][0]
+    mu = {c["method"]: c for c in ref_runs["cases"] if c["kind"] == "roots_muller"}
+    ii = [c for c in ref_runs["cases"] if c["kind"] == "inverse_iteration"]
+    z0 = ms.halton_points(ab["dom"], ab["nseed"])
+    lines = [f"roots 0 {ab['d']} {ab['n']} {ab['seed']} {ab['maxit']} {ab['toler']!r} {len(z0)} "
+             + " ".join(repr(v) for v in ab["dom"]) + " " + zs(z0)]
+    for m, name in ((1, "mineigval"), (2, "invtraceinv")):
+        c = mu[name]
+        z = cplx(c["z0"])
+        lines.append(f"roots {m} {c['d']} {c['n']} {c['seed']} {c['maxit']} {c['toler']!r} {len(z)} "
+                     + " ".join(repr(v) for v in c["dom"]) + " " + zs(z))
+    lines.append(f"eig 3 100 1 {len(ii)} " + zs([complex(*c["k"]) for c in ii]))
+    d, n, k, nx, ny, dom = 2, 60, 2.0 + 0.0j, 12, 10, [-6.0, 6.0, -5.0, 5.0]
+    lines.append(f"wave {d} {n} 1 3 {k.real!r} {k.imag!r} {nx} {ny} " + " ".join(repr(v) for v in dom))
+    out = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stdout[-2000:] + out.stderr[-2000:]
+    roots = {0: [], 1: [], 2: []}
+    nroot, states, vecs, wave = {}, {}, {}, {}
+    checked = None
+    for line in out.stdout.splitlines():
+        f = line.split()
+        if not f:
+            continue
+        if f[0] == "nroot":
+            nroot[int(f[1])] = (int(f[2]), float(f[3]))
+        elif f[0] == "root":
+            roots[int(f[1])].append(complex(float(f[3]), float(f[4])))
+        elif f[0] == "state":
+            states[int(f[1])] = (complex(float(f[2]), float(f[3])), complex(float(f[4]), float(f[5])))
+        elif f[0] == "vec":
+            vecs.setdefault(int(f[1]), []).append(complex(float(f[3]), float(f[4])))
+        elif f[0] == "wave":
+            wave[int(f[1])] = (float(f[2]), float(f[3]))
+        elif f[0] == "wave_pos0":
+            wave["pos0"] = [float(f[1]), float(f[2])]
+        elif f[0] == "checked":
+            checked = int(f[1])
+    # determinant method: the reference's root set; Muller methods: the same list in the same order
+    want = cplx(ab["roots"])
+    assert nroot[0][0] == len(want) and nroot[0][1] > 0
+    assert not match_root_sets(np.array(roots[0]), want, 1e-8)
+    for m, name in ((1, "mineigval"), (2, "invtraceinv")):
+        want = cplx(mu[name]["roots"])
+        got = np.array(roots[m])
+        assert len(got) == len(want), (name, got, want)
+        assert np.max(np.abs(got - want) / np.abs(want)) < 1e-8
+    # compute_eigenstates: every root's state through the reference's list functions
+    assert checked == len(ii)
+    for i, c in enumerate(ii):
+        kr, lam = states[i]
+        assert kr == complex(*c["k"])
+        if c["conv"]:
+            assert abs(lam - complex(*c["lam"])) < 1e-9
+            assert np.max(np.abs(np.array(vecs[i]) - cplx(c["vec"]))) < 1e-8
+        else:
+            assert abs(lam - complex(*c["lam"])) < 1e-6 * abs(complex(*c["lam"]))
+    # run_wave_function_omp: the average over seeds 1..3, med left holding seed 3
+    f_acc = np.zeros(nx * ny)
+    d_acc = np.zeros(nx * ny)
+    for s in (1, 2, 3):
+        _, p = oracle.wavefunction(d, n, oracle.fill_medium(d, n, s), k, nx, ny, dom)
+        f_acc += p.real
+        d_acc += np.abs(p) ** 2
+    fun = np.array([wave[l][0] for l in range(nx * ny)])
+    den = np.array([wave[l][1] for l in range(nx * ny)])
+    assert np.max(np.abs(fun - f_acc / 3)) < 1e-10 * np.max(np.abs(f_acc))
+    assert np.max(np.abs(den - d_acc / 3)) < 1e-9 * np.max(d_acc)
+    assert wave["pos0"] == list(oracle.fill_medium(d, n, 3)[:2])
