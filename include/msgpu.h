@@ -204,6 +204,14 @@ int msgpu_wave_function(int nmed, const msgpu_medium* media, const double* k, in
 int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, int nk, const double* ks, int nx, int ny,
                               const double* dom, double* function, double* density, double* psi, double* amps,
                               int precision);
+/* Wavefunction cut of run_wave_function_cut_omp (src/core/ms_core.c:654-703),
+ * plane wave along +x: every medium's amplitudes a = M^-1 phi in one batched
+ * job, then psi of each medium at the nbin points (xmin + i dx, 0, ...),
+ * dx = (xmax - xmin)/(nbin - 1) (get_pos_wfcut, init_wfcut):
+ * psi[2*(m*nbin + i)] complex; amps (may be NULL) as above.  Returns the OR of
+ * the solves' MSGPU_S_* words, or a negative MSGPU_E_* code. */
+int msgpu_wave_cut(int nmed, const msgpu_medium* media, const double* k, int nbin, double xmin, double xmax,
+                   double* psi, double* amps, int precision);
 
 /* Random function of run_random_function_omp (src/core/ms_core.c:476-519):
  * for every seed g < nseed (medium filled with seed g+1 by fill_medium) and

@@ -136,6 +136,22 @@ typedef struct msgpu_ref_wfun {
     double realtime;
 } msgpu_ref_wfun;
 
+/* reference WaveFunctionCut, src/core/wave_function_cut_type.h:20-38 */
+typedef struct msgpu_ref_wfcut {
+    int nseed;
+    uint64_t iseed;
+    msgpu_ref_iwave* iwave;
+    int nbin;
+    double xmin;
+    double xmax;
+    double dx;
+    int ntot;
+    double* repsi;
+    double* impsi;
+    double* density;
+    double realtime;
+} msgpu_ref_wfcut;
+
 /* reference Eigenstate, src/core/eigenstate_type.h:23-35 */
 typedef struct msgpu_ref_eigenstate {
     msgpu_dcomplex kroot;
@@ -208,6 +224,14 @@ void run_imag_mu_histogram_omp(msgpu_ref_medium* med, msgpu_ref_ihist* ihist, in
  * to their entry values divided by nseed, i.e. (entry + sum)/nseed as the
  * reference's sum and divide_wfun; med is left holding the last seed. */
 void run_wave_function_omp(msgpu_ref_medium* med, msgpu_ref_wfun* wfun, int nthread);
+/* replaces run_wave_function_cut_omp, src/core/ms_core.c:654-703, for the plane
+ * incident wave: psi of every seed iseed..iseed+nseed-1 on the cut in one
+ * batched GPU job (msgpu_wave_cut, mixed LU refined to an FP64 residual), the
+ * samples laid out bin-major as the reference's and handed to its own
+ * store_data_wfcut (weak reference, resolved from the program) for the means
+ * and quartiles.  med is left as it was, as the reference's private copies
+ * leave it. */
+void run_wave_function_cut_omp(msgpu_ref_medium* med, msgpu_ref_wfcut* wfcut, int nthread);
 /* replace find_eigenstates_serial_1/2/3, src/core/ms_core.c:320-401: the
  * resonance search on the realisation in eigls->med from the *nroot starting
  * points kroot, by the determinant (Aberth on dlogf, nexpsup = 4), mineigval or

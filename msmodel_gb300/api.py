@@ -85,6 +85,8 @@ def lib():
                                        C.c_void_p, C.c_int]
     L.msgpu_wave_function_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _dp, C.c_int, C.c_int, _dp, _dp,
                                              _dp, C.c_void_p, C.c_void_p, C.c_int]
+    L.msgpu_wave_cut.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, C.c_double, C.c_double, _dp, C.c_void_p,
+                                 C.c_int]
     L.msgpu_random_function.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(_Model), C.c_int,
                                          C.c_int, C.c_double, C.c_double, _dp, _ip, C.c_int]
     L.msgpu_traceinv_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip, C.c_int]
@@ -453,6 +455,55 @@ def wave_function_batch(media, ks, nx, ny, dom, precision="fp64", want_psi=True)
     a = amps.view(np.complex128).reshape(len(media), nk, n)
     return (fun.reshape(nk, npx), den.reshape(nk, npx),
             psi.view(np.complex128).reshape(nk, npx) if want_psi else None, [a[m].copy() for m in range(len(media))])
+
+
+def wave_cut(media, k, nbin, xmin, xmax, precision="fp64"):
+    """psi of every medium at the nbin points (xmin + i dx, 0, ...) of the x axis,
+    dx = (xmax - xmin)/(nbin - 1) (run_wave_function_cut_omp, ms_core.c:654-703;
+    get_pos_wfcut, wave_function_cut_util.c:83), all solves in one batched job.
+    Returns psi[nmed, nbin] (complex)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    psi = np.zeros(2 * len(media) * nbin)
+    kk = np.array([complex(k).real, complex(k).imag])
+    rc = lib().msgpu_wave_cut(len(media), _media_array(media), kk, nbin, float(xmin), float(xmax), psi, None,
+                              PRECISION[precision])
+    if rc < 0:
+        _check(rc, "wave_cut")
+    if rc > 0:
+        warnings.warn(f"wave_cut: a solve returned status {rc:#x} (singular or non-finite amplitudes)",
+                      RuntimeWarning, stacklevel=2)
+    return psi.view(np.complex128).reshape(len(media), nbin)
+
+
+def _mean_quartiles(samples):
+    """store_data_wfcut's statistics of one bin (wave_function_cut_util.c:92-114):
+    the samples sorted, their mean summed in order (mean_vector) and the first
+    and third quartiles by linear interpolation at (n-1) q (quantile,
+    real_vector_util.c:121-134)."""
+    x = np.sort(np.asarray(samples, dtype=np.float64))
+    n = x.size
+    out = [float(np.cumsum(x)[-1]) / n]
+    for q in (0.25, 0.75):
+        if n == 1:
+            out.append(float(x[0]))
+            continue
+        idx = (n - 1) * q
+        i = int(np.floor(idx))
+        out.append(float(x[i] + (idx - i) * (x[i + 1] - x[i])))
+    return out
+
+
+def run_wave_function_cut(media, k, nbin, xmin, xmax, precision="mixed"):
+    """run_wave_function_cut_omp (ms_core.c:654-703), plane wave, for the
+    realisations of media: psi of every seed on the cut on the GPU (wave_cut),
+    then per bin the mean and quartiles of Re psi, Im psi and |psi|^2 as
+    store_data_wfcut forms them.  Returns dict(repsi, impsi, density) with rows
+    [mean, q1/4, q3/4] per bin, and psi[nmed, nbin]."""
+    psi = wave_cut(media, k, nbin, xmin, xmax, precision)
+    out = {"psi": psi}
+    for key, v in (("repsi", psi.real), ("impsi", psi.imag), ("density", psi.real ** 2 + psi.imag ** 2)):
+        out[key] = np.array([_mean_quartiles(v[:, i]) for i in range(nbin)])
+    return out
 
 
 def solve_aberth_batch(media, dom, z0, nexpsup=4, maxit=30, toler=1e-10, precision="fp64"):

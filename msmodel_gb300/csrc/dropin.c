@@ -415,3 +415,53 @@ void compute_eigenstates(msgpu_ref_eigls* eigls, int nroot, msgpu_dcomplex* kroo
     printf("Done\n");
     check_eigenstate_list(eigls);
 }
+
+extern void store_data_wfcut(msgpu_ref_wfcut* wfcut, double* re, double* im, double* den) __attribute__((weak));
+
+void run_wave_function_cut_omp(msgpu_ref_medium* med, msgpu_ref_wfcut* wc, int nthread) {
+    (void)nthread;
+    if (!store_data_wfcut) {
+        printf("[ERROR] run_wave_function_cut_omp: the reference's store_data_wfcut is not linked in.\n");
+        return;
+    }
+    if (wc->iwave->source != 0) {
+        printf("[ERROR] run_wave_function_cut_omp: libmsgpu builds the plane incident wave only.\n");
+        return;
+    }
+    struct timespec t0;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int d = med->d, n = med->n, ns = wc->nseed, nb = wc->nbin;
+    if (ns < 1 || nb < 2) return;
+    msgpu_model mdl = to_model(med->scmodel);
+    msgpu_medium* media = (msgpu_medium*)calloc((size_t)ns, sizeof(msgpu_medium));
+    double* pos = (double*)malloc(sizeof(double) * (size_t)ns * n * d);
+    double* psi = (double*)malloc(sizeof(double) * 2 * (size_t)ns * nb);
+    double* re = (double*)malloc(sizeof(double) * (size_t)ns * nb);
+    double* im = (double*)malloc(sizeof(double) * (size_t)ns * nb);
+    double* den = (double*)malloc(sizeof(double) * (size_t)ns * nb);
+    for (int s = 0; s < ns; s++) {
+        double* p = pos + (size_t)s * n * d;
+        int e = msgpu_fill_medium(d, n, med->shape, med->ratio, wc->iseed + (uint64_t)s, p);
+        if (e) fail("run_wave_function_cut_omp: fill_medium", e);
+        media[s].d = d;
+        media[s].n = n;
+        media[s].pos = p;
+        media[s].model = mdl;
+    }
+    const double k[2] = {creal(wc->iwave->k), cimag(wc->iwave->k)};
+    int st = msgpu_wave_cut(ns, media, k, nb, wc->xmin, wc->xmax, psi, NULL, MSGPU_MIXED);
+    if (st < 0) fail("run_wave_function_cut_omp", st);
+    if (st & (MSGPU_S_SINGULAR | MSGPU_S_NONFINITE))
+        printf("[WARN] run_wave_function_cut_omp: a singular or non-finite solve reached the samples (status %d).\n",
+               st);
+    for (int s = 0; s < ns; s++)  /* bin-major samples, [s + i*nseed] (ms_core.c:687-689) */
+        for (int i = 0; i < nb; i++) {
+            const double a = psi[2 * ((size_t)s * nb + i)], b = psi[2 * ((size_t)s * nb + i) + 1];
+            re[s + (size_t)i * ns] = a;
+            im[s + (size_t)i * ns] = b;
+            den[s + (size_t)i * ns] = a * a + b * b;
+        }
+    store_data_wfcut(wc, re, im, den);
+    wc->realtime = seconds_since(&t0);
+    free(media); free(pos); free(psi); free(re); free(im); free(den);
+}

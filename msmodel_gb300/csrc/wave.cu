@@ -239,3 +239,93 @@ extern "C" int msgpu_wave_function(int nmed, const msgpu_medium* media, const do
                                    double* amps, int precision) {
     return msgpu_wave_function_batch(nmed, media, 1, k, nx, ny, dom, function, density, psi, amps, precision);
 }
+
+// Wavefunction cut of run_wave_function_cut_omp (src/core/ms_core.c:654-703):
+// every medium's amplitudes in one job, then psi at the nbin points
+// (xmin + i dx, 0, ...) of the x axis (get_pos_wfcut, wave_function_cut_util.c:83,
+// dx = (xmax - xmin)/(nbin - 1) as init_wfcut sets it) per medium: the grid
+// kernel on a one-row grid, each medium writing its own row of psi.
+extern "C" int msgpu_wave_cut(int nmed, const msgpu_medium* media, const double* k, int nbin, double xmin,
+                              double xmax, double* psi, double* amps, int precision) {
+    using namespace msg;
+    if (nmed < 1 || !media || !k || nbin < 2 || !psi) return MSGPU_E_ARG;
+    const int n = media[0].n, d = media[0].d;
+    for (int m = 0; m < nmed; ++m)
+        if (media[m].n != n || media[m].d != d || !media[m].pos) return MSGPU_E_ARG;
+    if ((size_t)nmed * nbin > (size_t)1 << 31) return MSGPU_E_SIZE;
+    std::vector<double> iks(2 * (size_t)nmed), sig(2 * (size_t)nmed), a(2 * (size_t)nmed * n);
+    std::vector<int> im(nmed), st(nmed);
+    for (int m = 0; m < nmed; ++m) {
+        iks[2 * m] = k[0];
+        iks[2 * m + 1] = k[1];
+        im[m] = m;
+    }
+    int e = msgpu_amplitude_batch(nmed, media, nmed, im.data(), iks.data(), sig.data(), a.data(), st.data(),
+                                  precision);
+    if (e) return e;
+    if (amps) std::copy(a.begin(), a.end(), amps);
+    // every medium's positions in one array; the double-float Green function needs |Im k| * r < 80
+    std::vector<double> pos((size_t)nmed * n * d);
+    double lo[3] = {std::min(xmin, xmax), 0.0, 0.0}, hi[3] = {std::max(xmin, xmax), 0.0, 0.0};
+    for (int m = 0; m < nmed; ++m) {
+        std::copy(media[m].pos, media[m].pos + (size_t)n * d, pos.begin() + (size_t)m * n * d);
+        if (d == 3)
+            for (int i = 0; i < n; ++i)
+                for (int c = 0; c < 3; ++c) {
+                    lo[c] = std::min(lo[c], media[m].pos[3 * i + c]);
+                    hi[c] = std::max(hi[c], media[m].pos[3 * i + c]);
+                }
+    }
+    const double rmax = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                  (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    const bool use_df = d == 3 && precision == MSGPU_MIXED && std::fabs(k[1]) * rmax < 80.0;
+    double *dpos = nullptr, *damp = nullptr, *dks = nullptr, *dfun = nullptr, *dden = nullptr, *dpsi = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dpos); cudaFree(damp); cudaFree(dks); cudaFree(dfun); cudaFree(dden); cudaFree(dpsi);
+    };
+    const size_t rows = (size_t)nmed * nbin;
+    if (cudaMalloc(&dpos, sizeof(double) * pos.size()) || cudaMalloc(&damp, sizeof(double) * a.size()) ||
+        cudaMalloc(&dks, sizeof(double) * 2) || cudaMalloc(&dfun, sizeof(double) * nbin) ||
+        cudaMalloc(&dden, sizeof(double) * nbin) || cudaMalloc(&dpsi, sizeof(double) * 2 * rows)) {
+        cleanup();
+        return MSGPU_E_CUDA;
+    }
+    if (cudaMemcpy(dpos, pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(damp, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(dks, k, sizeof(double) * 2, cudaMemcpyHostToDevice) ||
+        cudaMemset(dfun, 0, sizeof(double) * nbin) || cudaMemset(dden, 0, sizeof(double) * nbin)) {
+        cleanup();
+        return MSGPU_E_CUDA;
+    }
+    GridArgs A;
+    A.d = d;
+    A.n = n;
+    A.nx = nbin;
+    A.ny = 1;
+    A.ks = dks;
+    A.xmin = xmin;
+    A.dx = (xmax - xmin) / (nbin - 1);
+    A.ymax = 0.0;
+    A.dy = 0.0;
+    A.fun = dfun;  // the grid kernels' sums over media, not read
+    A.den = dden;
+    const dim3 grid((unsigned)((nbin + PT - 1) / PT), 1u);
+    for (int m = 0; m < nmed; ++m) {
+        A.pos = dpos + (size_t)m * n * d;
+        A.amp = damp + 2 * (size_t)m * n;
+        A.psi = dpsi + 2 * (size_t)m * nbin;
+        if (use_df) k_psi_grid_df3<<<grid, PT>>>(A);
+        else k_psi_grid<<<grid, PT>>>(A);
+        count_launches(1);
+        if (cudaGetLastError() != cudaSuccess) {
+            cleanup();
+            return MSGPU_E_CUDA;
+        }
+    }
+    const cudaError_t ce = cudaMemcpy(psi, dpsi, sizeof(double) * 2 * rows, cudaMemcpyDeviceToHost);
+    cleanup();
+    if (ce != cudaSuccess) return MSGPU_E_CUDA;
+    int any = 0;
+    for (int v : st) any |= v;
+    return any;
+}

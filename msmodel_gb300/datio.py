@@ -20,6 +20,7 @@ appends the section it names with the same keys, order and number formats:
   [wavefunction]     save_wfun             src/core/wave_function_util.c:228-245
                      (k and source: save_iwave, incident_wave_util.c:101;
                      function=/density=: save_real_data, real_vector_util.c:166)
+  [wavefunction_cut] save_wfcut            src/core/wave_function_cut_util.c:211-226
   data= line         save_cdata            src/core/complex_data_util.c:21-28
 
 `parse_cdata` reads a data= line back (parse_complex_data,
@@ -32,7 +33,7 @@ import numpy as np
 
 __all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
            "save_random_function", "save_eigenstate_list", "save_muplane", "save_imag_mu", "save_wavefunction",
-           "save_logcut"]
+           "save_wavefunction_cut", "save_logcut"]
 
 MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
@@ -187,3 +188,17 @@ def save_wavefunction(fname, function, density, nx, ny, dom, k, nseed, iseed=1, 
     text += _colorrule("color1", color1) + _colorrule("color2", color2)
     text += _real_data("function", function) + _real_data("density", density) + "\n"
     _append(fname, text)
+
+
+def save_wavefunction_cut(fname, stats, nbin, xmin, xmax, k, nseed, iseed=1, source="plane", realtime=0.0):
+    """A [wavefunction_cut] section: per bin of the cut the mean, first and third
+    quartiles of Re psi, Im psi and |psi|^2 over the seeds (stats as
+    run_wave_function_cut returns it: "repsi", "impsi", "density", nbin rows of
+    three), for the incident wave of wave number k."""
+    k = complex(k)
+    text = "[wavefunction_cut]\nnseed=%d\niseed=%d\nnbin=%d\n" % (nseed, iseed, nbin)
+    text += "xrange=%.16g:%.16g\n" % (xmin, xmax)
+    text += "k=%.16g%+.16gi\nsource=%s\nrealtime=%g\n" % (k.real, k.imag, source, realtime)
+    for key in ("repsi", "impsi", "density"):
+        text += _real_data(key, np.asarray(stats[key], dtype=np.float64).reshape(-1))
+    _append(fname, text + "\n")

@@ -253,6 +253,9 @@ class Reference:
                                           C.c_char_p, C.c_char_p, C.c_double, C.c_char_p]
         L.ref_inverse_iteration.argtypes = med + [_dp, _dp, _dp]
         L.ref_roots_muller.argtypes = [C.c_int] + med + [_dp, C.c_int, _dp, C.c_int, C.c_double]
+        L.ref_save_wfcut.argtypes = [C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_int, C.c_ulong, C.c_double,
+                                     _dp, _dp, _dp, C.c_char_p]
+        L.ref_wfcut_stats.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
 
     @staticmethod
@@ -394,6 +397,27 @@ class Reference:
                                      *self._med(d, n, model, params, shape, ratio, seed),
                                      np.asarray(dom, dtype=float), z.size // 2, z, maxit, toler)
         return z.view(np.complex128)[:nr].copy()
+
+    def save_wfcut(self, nbin, xmin, xmax, k, nseed, iseed, realtime, re, im, den, spherical=False):
+        """The text of the [wavefunction_cut] section save_wfcut writes for these statistics."""
+        import tempfile
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "wfcut.dat")
+            arr = [np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1)) for v in (re, im, den)]
+            self.L.ref_save_wfcut(nbin, xmin, xmax, np.array([k.real, k.imag]), int(spherical), nseed, iseed,
+                                  realtime, *arr, fname.encode())
+            with open(fname) as f:
+                return f.read()
+
+    def wfcut_stats(self, psi):
+        """store_data_wfcut on psi[nseed, nbin]: (repsi, impsi, density) rows
+        [mean, q1/4, q3/4] per bin, the reference's own arithmetic."""
+        psi = np.asarray(psi, dtype=np.complex128)
+        ns, nb = psi.shape
+        cols = [np.ascontiguousarray(v.T.reshape(-1)) for v in (psi.real, psi.imag, psi.real ** 2 + psi.imag ** 2)]
+        outs = [np.zeros(3 * nb) for _ in range(3)]
+        self.L.ref_wfcut_stats(ns, nb, *cols, *outs)
+        return tuple(o.reshape(nb, 3) for o in outs)
 
     def save_cdata(self, values, fname):
         z = np.ascontiguousarray(np.asarray(values, dtype=np.complex128))

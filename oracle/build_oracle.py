@@ -28,6 +28,8 @@ REF_SOURCES = [
     "imag_mu_histogram_util.c", "wave_function_util.c", "incident_wave_util.c",
     # the log cut's mesh and writer, and the incomplete gamma function its unit calls
     "log_cut_util.c", "incomplete_gamma.c", "classical_diffusion_util.c",
+    # the wavefunction cut's statistics (store_data_wfcut)
+    "wave_function_cut_util.c",
 ]
 
 

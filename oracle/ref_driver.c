@@ -30,6 +30,8 @@
 #include "incident_wave_util.h"
 #include "log_cut_type.h"
 #include "log_cut_util.h"
+#include "wave_function_cut_type.h"
+#include "wave_function_cut_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -425,4 +427,47 @@ void ref_logcut(int ns, double rek, double imkmin, double imkmax, int nseed, con
         save_logcut(&lc, fname);
     }
     del_logcut(&lc);
+}
+
+/* store_data_wfcut (wave_function_cut_util.c:92-114) on bin-major samples
+ * [s + i*nseed] of Re psi, Im psi and |psi|^2: out_*[3*i..3*i+2] = mean and
+ * the first and third quartiles of bin i, the reference's own statistics of
+ * run_wave_function_cut_omp (ms_core.c:695). */
+void ref_wfcut_stats(int nseed, int nbin, const double* re, const double* im, const double* den, double* out_re,
+                     double* out_im, double* out_den) {
+    WaveFunctionCut wc;
+    memset(&wc, 0, sizeof(wc));
+    wc.nseed = nseed;
+    wc.nbin = nbin;
+    wc.ntot = 3 * nbin;
+    wc.repsi = out_re;
+    wc.impsi = out_im;
+    wc.density = out_den;
+    const size_t m = (size_t)nseed * nbin;
+    double* a = (double*)malloc(sizeof(double) * m);
+    double* b = (double*)malloc(sizeof(double) * m);
+    double* c = (double*)malloc(sizeof(double) * m);
+    memcpy(a, re, sizeof(double) * m);
+    memcpy(b, im, sizeof(double) * m);
+    memcpy(c, den, sizeof(double) * m);
+    store_data_wfcut(&wc, a, b, c);
+    free(a); free(b); free(c);
+}
+
+/* save_wfcut (wave_function_cut_util.c:211-226): the [wavefunction_cut] section
+ * for these statistics (rows [mean, q1/4, q3/4] per bin, 3*nbin each) to fname */
+void ref_save_wfcut(int nbin, double xmin, double xmax, const double* k, int spherical_source, int nseed,
+                    unsigned long iseed, double realtime, const double* re, const double* im, const double* den,
+                    const char* fname) {
+    IncidentWave iw;
+    init_iwave(&iw, spherical_source ? spherical : plane, k[0] + I * k[1]);
+    WaveFunctionCut wc;
+    memset(&wc, 0, sizeof(wc));
+    init_wfcut(&wc, nbin, xmin, xmax, nseed, iseed, &iw);
+    wc.realtime = realtime;
+    memcpy(wc.repsi, re, sizeof(double) * 3 * (size_t)nbin);
+    memcpy(wc.impsi, im, sizeof(double) * 3 * (size_t)nbin);
+    memcpy(wc.density, den, sizeof(double) * 3 * (size_t)nbin);
+    save_wfcut(&wc, fname);
+    del_wfcut(&wc);
 }

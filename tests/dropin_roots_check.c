@@ -1,11 +1,12 @@
 /* Calls the eigenstate and wavefunction drop-ins (find_eigenstates_serial_1/2/3,
- * compute_eigenstates, run_wave_function_omp) the way the reference's
+ * compute_eigenstates, run_wave_function_omp, run_wave_function_cut_omp) the way the reference's
  * run_eigenstate_list_serial and ms_core_main call them, on cases read from
  * standard input, and prints the results for tests/test_gpu_dropin.py.
  *
  *   roots <method 0|1|2> d n seed maxit toler nz xmin xmax ymin ymax z0re z0im ...
  *   eig d n seed nk kre kim ...
  *   wave d n iseed nseed kre kim nx ny xmin xmax ymin ymax
+ *   cut d n iseed nseed kre kim nbin xmin xmax
  */
 #include <complex.h>
 #include <stdio.h>
@@ -27,6 +28,16 @@ void alloc_eigenstate_list(msgpu_ref_eigls* e, int nstate) {
 
 void check_eigenstate_list(msgpu_ref_eigls* e) {
     printf("checked %d\n", e->nstate);
+}
+
+/* stands in for the reference's store_data_wfcut (wave_function_cut_util.c:92),
+ * which the drop-in run_wave_function_cut_omp calls: prints the bin-major samples */
+void store_data_wfcut(msgpu_ref_wfcut* wc, double* re, double* im, double* den) {
+    for (int i = 0; i < wc->nbin; i++)
+        for (int s = 0; s < wc->nseed; s++) {
+            const size_t o = (size_t)s + (size_t)i * wc->nseed;
+            printf("cut %d %d %.17g %.17g %.17g\n", s, i, re[o], im[o], den[o]);
+        }
 }
 
 static msgpu_ref_scmodel sm;
@@ -142,6 +153,31 @@ int main(void) {
             printf("wave_realtime %.6g\n", wf.realtime);
             free(wf.function);
             free(wf.density);
+            free(med.pos);
+        } else if (!strcmp(cmd, "cut")) {
+            int d, n, nseed, nbin;
+            unsigned long iseed;
+            double kre, kim, xmin, xmax;
+            if (scanf("%d %d %lu %d %lf %lf %d %lf %lf", &d, &n, &iseed, &nseed, &kre, &kim, &nbin, &xmin, &xmax) != 9)
+                return 2;
+            msgpu_ref_medium med = make_medium(d, n, 7);
+            const double p0 = med.pos[0];
+            msgpu_ref_iwave iw;
+            memset(&iw, 0, sizeof(iw));
+            iw.k = kre + I * kim;
+            msgpu_ref_wfcut wc;
+            memset(&wc, 0, sizeof(wc));
+            wc.nseed = nseed;
+            wc.iseed = iseed;
+            wc.iwave = &iw;
+            wc.nbin = nbin;
+            wc.xmin = xmin;
+            wc.xmax = xmax;
+            wc.dx = (xmax - xmin) / (nbin - 1);
+            wc.ntot = 3 * nbin;
+            run_wave_function_cut_omp(&med, &wc, 4);
+            printf("cut_med_kept %d\n", med.pos[0] == p0);
+            printf("cut_realtime %.6g\n", wc.realtime);
             free(med.pos);
         } else {
             return 2;

@@ -167,6 +167,7 @@ def reference_runs():
         add("eigvals", d=d, n=n, seed=seed, k=[k.real, k.imag], mu=_cl(r.eigvals(d, n, seed, k)))
     runs["cases"].extend(chistogram_cases(r))
     runs["cases"].extend(logcut_cases(r))
+    runs["cases"].extend(wfcut_cases(r))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
@@ -236,6 +237,28 @@ def logcut_cases(r):
              "text": text}]
 
 
+def wfcut_cases(r):
+    """The wavefunction cut's statistics (store_data_wfcut, wave_function_cut_util.c:92-114,
+    called by run_wave_function_cut_omp, ms_core.c:695): mean and quartiles per bin of
+    seeded psi samples, including one seed, two seeds and tied samples."""
+    rng = np.random.default_rng(11)
+    out = []
+    for ns, nb in ((1, 3), (2, 4), (9, 5), (40, 6)):
+        psi = rng.standard_normal((ns, nb)) + 1j * rng.standard_normal((ns, nb))
+        if ns >= 9:
+            psi[3, :] = psi[1, :]  # ties
+        re, im, den = r.wfcut_stats(psi)
+        out.append({"kind": "wfcut_stats", "nseed": ns, "nbin": nb, "psi": [_cl(row) for row in psi],
+                    "repsi": re.tolist(), "impsi": im.tolist(), "density": den.tolist()})
+    # the [wavefunction_cut] section save_wfcut writes for the last statistics
+    k = complex(1.5, -0.01)
+    text = r.save_wfcut(nb, -8.0, 8.0, k, ns, 2, 3.25, re, im, den)
+    out.append({"kind": "wavefunction_cut_file", "nbin": nb, "xmin": -8.0, "xmax": 8.0, "k": [k.real, k.imag],
+                "nseed": ns, "iseed": 2, "realtime": 3.25, "repsi": re.tolist(), "impsi": im.tolist(),
+                "density": den.tolist(), "text": text})
+    return out
+
+
 if __name__ == "__main__":
     if "--chistogram-only" in sys.argv:
         # add or refresh only the mu-plane histogram cases of an existing reference_runs.json
@@ -245,8 +268,9 @@ if __name__ == "__main__":
             runs = json.load(f)
         r = Reference()
         runs["cases"] = [c for c in runs["cases"] if c["kind"] not in ("chistogram", "imag_mu", "wavefunction_file",
-                                                                       "logcut")
-                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r)
+                                                                       "logcut", "wfcut_stats",
+                                                                       "wavefunction_cut_file")
+                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r) + wfcut_cases(r)
         with open(path, "w") as f:
             json.dump(runs, f, indent=0)
         sys.exit(0)

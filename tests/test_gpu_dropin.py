@@ -146,6 +146,8 @@ def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
     lines.append(f"eig 3 100 1 {len(ii)} " + zs([complex(*c["k"]) for c in ii]))
     d, n, k, nx, ny, dom = 2, 60, 2.0 + 0.0j, 12, 10, [-6.0, 6.0, -5.0, 5.0]
     lines.append(f"wave {d} {n} 1 3 {k.real!r} {k.imag!r} {nx} {ny} " + " ".join(repr(v) for v in dom))
+    kc, nbin, xmin, xmax = 1.5 - 0.01j, 17, -8.0, 8.0
+    lines.append(f"cut 3 60 2 3 {kc.real!r} {kc.imag!r} {nbin} {xmin!r} {xmax!r}")
     out = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stdout[-2000:] + out.stderr[-2000:]
     roots = {0: [], 1: [], 2: []}
@@ -169,6 +171,10 @@ def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
             wave["pos0"] = [float(f[1]), float(f[2])]
         elif f[0] == "checked":
             checked = int(f[1])
+        elif f[0] == "cut":
+            wave[("cut", int(f[1]), int(f[2]))] = complex(float(f[3]), float(f[4]))
+        elif f[0] == "cut_med_kept":
+            wave["cut_med_kept"] = int(f[1])
     # determinant method: the reference's root set; Muller methods: the same list in the same order
     want = cplx(ab["roots"])
     assert nroot[0][0] == len(want) and nroot[0][1] > 0
@@ -200,3 +206,11 @@ def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
     assert np.max(np.abs(fun - f_acc / 3)) < 1e-10 * np.max(np.abs(f_acc))
     assert np.max(np.abs(den - d_acc / 3)) < 1e-9 * np.max(d_acc)
     assert wave["pos0"] == list(oracle.fill_medium(d, n, 3)[:2])
+    # run_wave_function_cut_omp: psi of seeds 2..4 on the cut, handed bin-major to store_data_wfcut;
+    # the caller's medium untouched
+    for s in range(3):
+        pos = oracle.fill_medium(3, 60, 2 + s)
+        want = oracle.wavefunction(3, 60, pos, kc, nbin, 2, [xmin, xmax, -1.0, 0.0])[1][:nbin]
+        got = np.array([wave[("cut", s, i)] for i in range(nbin)])
+        assert np.max(np.abs(got - want)) < 1e-10 * np.max(np.abs(want))
+    assert wave["cut_med_kept"] == 1

@@ -88,3 +88,22 @@ def test_wave_singular_solve_is_reported(ms):
     with warnings.catch_warnings():
         warnings.simplefilter("error")
         ms.wave_function_batch([med], [1.5 + 0j], 8, 8, dom, want_psi=False)
+
+
+@pytest.mark.parametrize("d,precision", [(3, "fp64"), (3, "mixed"), (2, "fp64")])
+def test_wave_cut_matches_oracle(ms, oracle, d, precision):
+    """run_wave_function_cut_omp's samples: psi of every seed at the nbin points
+    (xmin + i dx, 0, ...), against the oracle's psi on the y = 0 row of a grid;
+    then the per-bin mean and quartiles of those samples."""
+    n, k, nbin, xmin, xmax = 60, 1.5 - 0.01j, 33, -8.0, 8.0
+    media = [ms.Medium(d, n, seed=s) for s in (1, 2, 3, 4)]
+    psi = ms.wave_cut(media, k, nbin, xmin, xmax, precision)
+    want = np.array([oracle.wavefunction(d, n, m.pos, k, nbin, 2, [xmin, xmax, -1.0, 0.0])[1][:nbin]
+                     for m in media])
+    assert psi.shape == (4, nbin)
+    assert np.max(np.abs(psi - want)) < 1e-10 * np.max(np.abs(want))
+    st = ms.run_wave_function_cut(media, k, nbin, xmin, xmax, precision)
+    from msmodel_gb300.api import _mean_quartiles
+    for key, v in (("repsi", want.real), ("impsi", want.imag), ("density", np.abs(want) ** 2)):
+        ref = np.array([_mean_quartiles(v[:, i]) for i in range(nbin)])
+        assert np.max(np.abs(st[key] - ref)) < 1e-9 * np.max(np.abs(ref)), key
