@@ -212,6 +212,16 @@ int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, int nk, const
  * the solves' MSGPU_S_* words, or a negative MSGPU_E_* code. */
 int msgpu_wave_cut(int nmed, const msgpu_medium* media, const double* k, int nbin, double xmin, double xmax,
                    double* psi, double* amps, int precision);
+/* Differential cross section of run_differential_cross_section_omp
+ * (src/core/ms_core.c:526-594) at real k, plane wave along +x: every medium's
+ * amplitudes a in one batched job, then for the nbin angles
+ * th_i = thmin exp(i log(thmax/thmin)/(nbin-1)) degrees (get_arg_dcs,
+ * diff_cross_section_util.c:86; thmin, thmax > 0) the far-field sample
+ * (k/2pi)^(d-3)/(16 pi^2) |sum_j conj(b_j) a_j|^2, b the plane wave of
+ * direction th_i (build_plane_wave), into samples[m + i*nmed] (nmed <= 65535).
+ * Returns the OR of the solves' MSGPU_S_* words, or a negative MSGPU_E_* code. */
+int msgpu_diff_cross_section(int nmed, const msgpu_medium* media, double k, int nbin, double thmin, double thmax,
+                             double* samples, int precision);
 
 /* Random function of run_random_function_omp (src/core/ms_core.c:476-519):
  * for every seed g < nseed (medium filled with seed g+1 by fill_medium) and

@@ -152,6 +152,24 @@ typedef struct msgpu_ref_wfcut {
     double realtime;
 } msgpu_ref_wfcut;
 
+/* reference DiffCrossSection, src/core/diff_cross_section_type.h:15-31 */
+typedef struct msgpu_ref_dcs {
+    int nseed;
+    uint64_t iseed;
+    double k;
+    double thmin;
+    double thmax;
+    int nbin;
+    int nq;
+    int ntot;
+    double* data;
+    double* mean;
+    int nc;
+    double* curve;
+    char title[80];
+    double realtime;
+} msgpu_ref_dcs;
+
 /* reference Eigenstate, src/core/eigenstate_type.h:23-35 */
 typedef struct msgpu_ref_eigenstate {
     msgpu_dcomplex kroot;
@@ -232,6 +250,13 @@ void run_wave_function_omp(msgpu_ref_medium* med, msgpu_ref_wfun* wfun, int nthr
  * and quartiles.  med is left as it was, as the reference's private copies
  * leave it. */
 void run_wave_function_cut_omp(msgpu_ref_medium* med, msgpu_ref_wfcut* wfcut, int nthread);
+/* replaces run_differential_cross_section_omp, src/core/ms_core.c:526-594: the
+ * samples of seeds iseed..iseed+nseed-1 in one batched GPU job
+ * (msgpu_diff_cross_section, mixed LU refined to an FP64 residual), then the
+ * reference's statistics in its order: the first nc seeds' curves, each bin's
+ * samples sorted, its nq quantiles at q/(nq-1) and its mean (real_vector_util.c
+ * quantile and mean_vector).  med is left as it was. */
+void run_differential_cross_section_omp(msgpu_ref_medium* med, msgpu_ref_dcs* dcs, int nthread);
 /* replace find_eigenstates_serial_1/2/3, src/core/ms_core.c:320-401: the
  * resonance search on the realisation in eigls->med from the *nroot starting
  * points kroot, by the determinant (Aberth on dlogf, nexpsup = 4), mineigval or

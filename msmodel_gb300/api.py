@@ -87,6 +87,8 @@ def lib():
                                              _dp, C.c_void_p, C.c_void_p, C.c_int]
     L.msgpu_wave_cut.argtypes = [C.c_int, C.POINTER(_Medium), _dp, C.c_int, C.c_double, C.c_double, _dp, C.c_void_p,
                                  C.c_int]
+    L.msgpu_diff_cross_section.argtypes = [C.c_int, C.POINTER(_Medium), C.c_double, C.c_int, C.c_double, C.c_double,
+                                           _dp, C.c_int]
     L.msgpu_random_function.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(_Model), C.c_int,
                                          C.c_int, C.c_double, C.c_double, _dp, _ip, C.c_int]
     L.msgpu_traceinv_batch.argtypes = [C.c_int, C.POINTER(_Medium), C.c_int, _ip, _dp, _dp, _ip, C.c_int]
@@ -475,22 +477,30 @@ def wave_cut(media, k, nbin, xmin, xmax, precision="fp64"):
     return psi.view(np.complex128).reshape(len(media), nbin)
 
 
+def _quantile_sorted(x, q):
+    """quantile (real_vector_util.c:121-134) of sorted samples x: linear
+    interpolation at the continuous index (n-1) q."""
+    n = x.size
+    if n == 1 or q <= 0.0:
+        return float(x[0])
+    if q >= 1.0:
+        return float(x[n - 1])
+    idx = (n - 1) * q
+    i = int(math.floor(idx))
+    return float(x[i] + (idx - i) * (x[i + 1] - x[i]))
+
+
+def _mean_sorted(x):
+    """mean_vector (real_vector_util.c:139-147): the sum in order over n."""
+    return float(np.cumsum(x)[-1]) / x.size
+
+
 def _mean_quartiles(samples):
     """store_data_wfcut's statistics of one bin (wave_function_cut_util.c:92-114):
     the samples sorted, their mean summed in order (mean_vector) and the first
-    and third quartiles by linear interpolation at (n-1) q (quantile,
-    real_vector_util.c:121-134)."""
+    and third quartiles (quantile)."""
     x = np.sort(np.asarray(samples, dtype=np.float64))
-    n = x.size
-    out = [float(np.cumsum(x)[-1]) / n]
-    for q in (0.25, 0.75):
-        if n == 1:
-            out.append(float(x[0]))
-            continue
-        idx = (n - 1) * q
-        i = int(np.floor(idx))
-        out.append(float(x[i] + (idx - i) * (x[i + 1] - x[i])))
-    return out
+    return [_mean_sorted(x), _quantile_sorted(x, 0.25), _quantile_sorted(x, 0.75)]
 
 
 def run_wave_function_cut(media, k, nbin, xmin, xmax, precision="mixed"):
@@ -503,6 +513,49 @@ def run_wave_function_cut(media, k, nbin, xmin, xmax, precision="mixed"):
     out = {"psi": psi}
     for key, v in (("repsi", psi.real), ("impsi", psi.imag), ("density", psi.real ** 2 + psi.imag ** 2)):
         out[key] = np.array([_mean_quartiles(v[:, i]) for i in range(nbin)])
+    return out
+
+
+def diff_cross_section(media, k, nbin, thmin, thmax, precision="fp64"):
+    """The differential cross section samples of run_differential_cross_section_omp
+    (ms_core.c:526-594) at real k for every medium, all solves in one batched job:
+    samples[i, m] = (k/2pi)^(d-3)/(16 pi^2) |b(th_i)^H a_m|^2 at the angles
+    th_i = thmin exp(i log(thmax/thmin)/(nbin-1)) degrees (get_arg_dcs)."""
+    media = [media] if isinstance(media, Medium) else list(media)
+    out = np.zeros(len(media) * nbin)
+    rc = lib().msgpu_diff_cross_section(len(media), _media_array(media), float(k), nbin, float(thmin), float(thmax),
+                                        out, PRECISION[precision])
+    if rc < 0:
+        _check(rc, "diff_cross_section")
+    if rc > 0:
+        warnings.warn(f"diff_cross_section: a solve returned status {rc:#x} (singular or non-finite amplitudes)",
+                      RuntimeWarning, stacklevel=2)
+    return out.reshape(nbin, len(media))
+
+
+def dcs_statistics(samples, nq, nc):
+    """The statistics run_differential_cross_section_omp forms from samples[nbin,
+    nseed] (ms_core.c:568-583): curve[i, s] the first nc seeds' samples, then per
+    bin the samples sorted, data[i, q] their quantile at q/(nq-1) and mean[i]."""
+    samples = np.asarray(samples, dtype=np.float64)
+    nbin = samples.shape[0]
+    curve = samples[:, :nc].copy()
+    data = np.zeros((nbin, nq))
+    mean = np.zeros(nbin)
+    for i in range(nbin):
+        x = np.sort(samples[i])
+        data[i] = [_quantile_sorted(x, q / (nq - 1)) for q in range(nq)]
+        mean[i] = _mean_sorted(x)
+    return {"data": data, "mean": mean, "curve": curve}
+
+
+def run_differential_cross_section(media, k, nbin, thmin, thmax, nq=5, nc=1, precision="mixed"):
+    """run_differential_cross_section_omp for the realisations of media (seeds in
+    order): the samples on the GPU (diff_cross_section), then dcs_statistics.
+    Returns dict(samples, data, mean, curve)."""
+    samples = diff_cross_section(media, k, nbin, thmin, thmax, precision)
+    out = dcs_statistics(samples, nq, nc)
+    out["samples"] = samples
     return out
 
 

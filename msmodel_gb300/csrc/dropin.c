@@ -465,3 +465,63 @@ void run_wave_function_cut_omp(msgpu_ref_medium* med, msgpu_ref_wfcut* wc, int n
     wc->realtime = seconds_since(&t0);
     free(media); free(pos); free(psi); free(re); free(im); free(den);
 }
+
+static int cmp_double(const void* a, const void* b) {
+    const double x = *(const double*)a, y = *(const double*)b;
+    return (x > y) - (x < y);
+}
+
+/* quantile (real_vector_util.c:121-134) of n sorted samples: linear
+ * interpolation at the continuous index (n-1) q */
+static double quantile_sorted(int n, const double* x, double q) {
+    if (n <= 0) return NAN;
+    if (n == 1 || q <= 0.) return x[0];
+    if (q >= 1.) return x[n - 1];
+    const double idx = (n - 1) * q;
+    const int i = (int)floor(idx);
+    return x[i] + (idx - i) * (x[i + 1] - x[i]);
+}
+
+void run_differential_cross_section_omp(msgpu_ref_medium* med, msgpu_ref_dcs* dcs, int nthread) {
+    (void)nthread;
+    if (med->d == 1)  /* the reference's own warning, ms_core.c:527-528 */
+        printf("[WARN] The differential cross section in %dD cannot be computed in the same way as in other "
+               "dimensions. This may lead to strange results...\n", med->d);
+    struct timespec t0;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    const int d = med->d, n = med->n, ns = dcs->nseed, nb = dcs->nbin;
+    if (ns < 1 || nb < 2) return;
+    msgpu_model mdl = to_model(med->scmodel);
+    msgpu_medium* media = (msgpu_medium*)calloc((size_t)ns, sizeof(msgpu_medium));
+    double* pos = (double*)malloc(sizeof(double) * (size_t)ns * n * d);
+    double* smp = (double*)malloc(sizeof(double) * (size_t)ns * nb);
+    for (int s = 0; s < ns; s++) {
+        double* p = pos + (size_t)s * n * d;
+        int e = msgpu_fill_medium(d, n, med->shape, med->ratio, dcs->iseed + (uint64_t)s, p);
+        if (e) fail("run_differential_cross_section_omp: fill_medium", e);
+        media[s].d = d;
+        media[s].n = n;
+        media[s].pos = p;
+        media[s].model = mdl;
+    }
+    int st = msgpu_diff_cross_section(ns, media, dcs->k, nb, dcs->thmin, dcs->thmax, smp, MSGPU_MIXED);
+    if (st < 0) fail("run_differential_cross_section_omp", st);
+    if (st & (MSGPU_S_SINGULAR | MSGPU_S_NONFINITE))
+        printf("[WARN] run_differential_cross_section_omp: a singular or non-finite solve reached the samples "
+               "(status %d).\n", st);
+    /* ms_core.c:568-583: sample curves of the first nc seeds (at most nseed of them:
+     * the reference's loop reads past its samples beyond that), then per bin the
+     * sorted samples' quantiles and mean */
+    for (int s = 0; s < dcs->nc && s < ns; s++)
+        for (int i = 0; i < nb; i++) dcs->curve[s + i * dcs->nc] = smp[s + (size_t)i * ns];
+    for (int i = 0; i < nb; i++) {
+        double* x = smp + (size_t)i * ns;
+        qsort(x, (size_t)ns, sizeof(double), cmp_double);
+        for (int q = 0; q < dcs->nq; q++) dcs->data[q + i * dcs->nq] = quantile_sorted(ns, x, ((double)q) / (dcs->nq - 1));
+        double sum = 0.;
+        for (int s = 0; s < ns; s++) sum += x[s];
+        dcs->mean[i] = sum / ns;
+    }
+    dcs->realtime = seconds_since(&t0);
+    free(media); free(pos); free(smp);
+}

@@ -21,6 +21,7 @@ appends the section it names with the same keys, order and number formats:
                      (k and source: save_iwave, incident_wave_util.c:101;
                      function=/density=: save_real_data, real_vector_util.c:166)
   [wavefunction_cut] save_wfcut            src/core/wave_function_cut_util.c:211-226
+  [diff_cross_section] save_diff_cross_section  src/core/diff_cross_section_util.c:259-284
   data= line         save_cdata            src/core/complex_data_util.c:21-28
 
 `parse_cdata` reads a data= line back (parse_complex_data,
@@ -33,7 +34,7 @@ import numpy as np
 
 __all__ = ["format_cdata", "parse_cdata", "save_medium", "save_complexmap", "save_complexcut",
            "save_random_function", "save_eigenstate_list", "save_muplane", "save_imag_mu", "save_wavefunction",
-           "save_wavefunction_cut", "save_logcut"]
+           "save_wavefunction_cut", "save_diff_cross_section", "save_logcut"]
 
 MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
@@ -202,3 +203,20 @@ def save_wavefunction_cut(fname, stats, nbin, xmin, xmax, k, nseed, iseed=1, sou
     for key in ("repsi", "impsi", "density"):
         text += _real_data(key, np.asarray(stats[key], dtype=np.float64).reshape(-1))
     _append(fname, text + "\n")
+
+
+def save_diff_cross_section(fname, dcs, k, nseed, iseed, thmin, thmax, title="", realtime=0.0):
+    """A [diff_cross_section] section: per bin the nq quantiles (data, rows of
+    nq), the mean and the first nc seeds' curves (curve, rows of nc), as
+    run_differential_cross_section returns them, at wave number k over the
+    angles thmin..thmax degrees."""
+    data = np.asarray(dcs["data"], dtype=np.float64)
+    curve = np.asarray(dcs["curve"], dtype=np.float64)
+    nbin, nq = data.shape
+    text = "[diff_cross_section]\ntitle=%s\nnseed=%d\niseed=%d\nk=%g\n" % (title, nseed, iseed, k)
+    text += "thmin=%s\nthmax=%s\nnbin=%d\nnq=%d\nrealtime=%s\n" % (_g16(thmin), _g16(thmax), nbin, nq,
+                                                                     _g16(realtime))
+    text += "data=" + "".join(_g16(v) + " " for v in data.reshape(-1))
+    text += "\nmean=" + "".join(_g16(v) + " " for v in np.asarray(dcs["mean"], dtype=np.float64))
+    text += "\nnc=%d\ncurve=" % curve.shape[1] + "".join(_g16(v) + " " for v in curve.reshape(-1)) + "\n\n"
+    _append(fname, text)

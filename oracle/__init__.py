@@ -255,6 +255,9 @@ class Reference:
         L.ref_roots_muller.argtypes = [C.c_int] + med + [_dp, C.c_int, _dp, C.c_int, C.c_double]
         L.ref_save_wfcut.argtypes = [C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_int, C.c_ulong, C.c_double,
                                      _dp, _dp, _dp, C.c_char_p]
+        L.ref_diff_cross_section.argtypes = med[:-1] + [C.c_double, C.c_int, C.c_ulong, C.c_int, C.c_double,
+                                                        C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_double,
+                                                        C.c_char_p, _dp, _dp, _dp, _dp]
         L.ref_wfcut_stats.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
 
@@ -408,6 +411,22 @@ class Reference:
                                   realtime, *arr, fname.encode())
             with open(fname) as f:
                 return f.read()
+
+    def diff_cross_section(self, d, n, k, nseed, iseed, nbin, thmin, thmax, nq, nc, title="", realtime=0.0,
+                           model="maximum", params=(), shape="ball", ratio=1.0):
+        """run_differential_cross_section_omp's arithmetic on one thread with the
+        reference's functions: (samples[nbin, nseed], data[nbin, nq], mean[nbin],
+        curve[nbin, nc], the [diff_cross_section] section text)."""
+        import tempfile
+        smp, data, mean, curve = np.zeros(nseed * nbin), np.zeros(nbin * nq), np.zeros(nbin), np.zeros(nbin * nc)
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "dcs.dat")
+            self.L.ref_diff_cross_section(*self._med(d, n, model, params, shape, ratio, 1)[:-1], float(k), nseed,
+                                          iseed, nbin, thmin, thmax, nq, nc, title.encode(), realtime,
+                                          fname.encode(), smp, data, mean, curve)
+            with open(fname) as f:
+                text = f.read()
+        return smp.reshape(nbin, nseed), data.reshape(nbin, nq), mean, curve.reshape(nbin, nc), text
 
     def wfcut_stats(self, psi):
         """store_data_wfcut on psi[nseed, nbin]: (repsi, impsi, density) rows

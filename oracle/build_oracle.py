@@ -30,6 +30,8 @@ REF_SOURCES = [
     "log_cut_util.c", "incomplete_gamma.c", "classical_diffusion_util.c",
     # the wavefunction cut's statistics (store_data_wfcut)
     "wave_function_cut_util.c",
+    # the differential cross section's angles and writer
+    "diff_cross_section_util.c",
 ]
 
 

@@ -32,6 +32,8 @@
 #include "log_cut_util.h"
 #include "wave_function_cut_type.h"
 #include "wave_function_cut_util.h"
+#include "diff_cross_section_type.h"
+#include "diff_cross_section_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -470,4 +472,61 @@ void ref_save_wfcut(int nbin, double xmin, double xmax, const double* k, int sph
     memcpy(wc.density, den, sizeof(double) * 3 * (size_t)nbin);
     save_wfcut(&wc, fname);
     del_wfcut(&wc);
+}
+
+/* run_differential_cross_section_omp (ms_core.c:526-594) on one thread with the
+ * reference's own steps in its order: per seed iseed + s, build_ms_matrix,
+ * build_plane_wave (theta = 0), zgesv_, then per bin get_arg_dcs,
+ * build_plane_wave, cdot_product and the prefactor; then the first nc curves,
+ * sort_vector, quantile and mean_vector.  samples[s + i*nseed] before the sort;
+ * data[q + i*nq], mean[i], curve[s + i*nc]; the [diff_cross_section] section
+ * save_diff_cross_section writes (title, realtime given) to fname. */
+void ref_diff_cross_section(int d, int n, int mtype, int np, const double* p, int shape, double ratio, double k,
+                            int nseed, unsigned long iseed, int nbin, double thmin, double thmax, int nq, int nc,
+                            const char* title, double realtime, const char* fname, double* samples, double* data,
+                            double* mean, double* curve) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, iseed);
+    DiffCrossSection dcs;
+    memset(&dcs, 0, sizeof(dcs));
+    char tt[80];
+    strncpy(tt, title, sizeof(tt) - 1);
+    tt[sizeof(tt) - 1] = '\0';
+    init_diff_cross_section(&dcs, nseed, iseed, k, nbin, nq, nc, thmin, thmax, tt);
+    const double PI_ = 3.1415926535897932385;
+    double prefac = pow(dcs.k / (2 * PI_), med.d - 3) / (16 * PI_ * PI_);
+    double* smp = (double*)calloc((size_t)nseed * nbin, sizeof(double));
+    dcomplex* m = (dcomplex*)calloc((size_t)n * n, sizeof(dcomplex));
+    dcomplex* a = (dcomplex*)calloc((size_t)n, sizeof(dcomplex));
+    dcomplex* b = (dcomplex*)calloc((size_t)n, sizeof(dcomplex));
+    int* ipiv = (int*)calloc((size_t)n, sizeof(int));
+    int nrhs = 1, info;
+    for (int s = 0; s < nseed; s++) {
+        fill_medium(&med, s + dcs.iseed);
+        build_ms_matrix(&med, dcs.k, m);
+        build_plane_wave(&med, dcs.k, 0., a);
+        zgesv_(&n, &nrhs, m, &n, ipiv, a, &n, &info);
+        for (int i = 0; i < nbin; i++) {
+            double theta = get_arg_dcs(&dcs, i);
+            build_plane_wave(&med, dcs.k, theta, b);
+            dcomplex atot = cdot_product(n, b, a);
+            smp[s + i * nseed] = prefac * (creal(atot) * creal(atot) + cimag(atot) * cimag(atot));
+        }
+    }
+    memcpy(samples, smp, sizeof(double) * (size_t)nseed * nbin);
+    for (int s = 0; s < dcs.nc; s++)
+        for (int i = 0; i < nbin; i++) dcs.curve[s + i * dcs.nc] = smp[s + i * nseed];
+    for (int i = 0; i < nbin; i++) {
+        sort_vector(nseed, smp + i * nseed);
+        for (int q = 0; q < dcs.nq; q++) dcs.data[q + i * dcs.nq] = quantile(nseed, smp + i * nseed, ((double)q) / (dcs.nq - 1));
+        dcs.mean[i] = mean_vector(nseed, smp + i * nseed);
+    }
+    dcs.realtime = realtime;
+    save_diff_cross_section(&dcs, fname);
+    memcpy(data, dcs.data, sizeof(double) * (size_t)nbin * nq);
+    memcpy(mean, dcs.mean, sizeof(double) * (size_t)nbin);
+    memcpy(curve, dcs.curve, sizeof(double) * (size_t)nbin * nc);
+    free(smp); free(m); free(a); free(b); free(ipiv);
+    del_diff_cross_section(&dcs);
+    drop_medium(&med);
 }

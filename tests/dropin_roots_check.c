@@ -1,5 +1,6 @@
 /* Calls the eigenstate and wavefunction drop-ins (find_eigenstates_serial_1/2/3,
- * compute_eigenstates, run_wave_function_omp, run_wave_function_cut_omp) the way the reference's
+ * compute_eigenstates, run_wave_function_omp, run_wave_function_cut_omp,
+ * run_differential_cross_section_omp) the way the reference's
  * run_eigenstate_list_serial and ms_core_main call them, on cases read from
  * standard input, and prints the results for tests/test_gpu_dropin.py.
  *
@@ -7,6 +8,7 @@
  *   eig d n seed nk kre kim ...
  *   wave d n iseed nseed kre kim nx ny xmin xmax ymin ymax
  *   cut d n iseed nseed kre kim nbin xmin xmax
+ *   dcs d n iseed nseed k nbin thmin thmax nq nc
  */
 #include <complex.h>
 #include <stdio.h>
@@ -178,6 +180,36 @@ int main(void) {
             run_wave_function_cut_omp(&med, &wc, 4);
             printf("cut_med_kept %d\n", med.pos[0] == p0);
             printf("cut_realtime %.6g\n", wc.realtime);
+            free(med.pos);
+        } else if (!strcmp(cmd, "dcs")) {
+            int d, n, nseed, nbin, nq, nc;
+            unsigned long iseed;
+            double k, thmin, thmax;
+            if (scanf("%d %d %lu %d %lf %d %lf %lf %d %d", &d, &n, &iseed, &nseed, &k, &nbin, &thmin, &thmax, &nq,
+                      &nc) != 10)
+                return 2;
+            msgpu_ref_medium med = make_medium(d, n, 7);
+            msgpu_ref_dcs dc;
+            memset(&dc, 0, sizeof(dc));
+            dc.nseed = nseed;
+            dc.iseed = iseed;
+            dc.k = k;
+            dc.thmin = thmin;
+            dc.thmax = thmax;
+            dc.nbin = nbin;
+            dc.nq = nq;
+            dc.ntot = nbin * nq;
+            dc.nc = nc;
+            dc.data = (double*)calloc((size_t)nbin * nq, sizeof(double));
+            dc.mean = (double*)calloc((size_t)nbin, sizeof(double));
+            dc.curve = (double*)calloc((size_t)nbin * nc, sizeof(double));
+            run_differential_cross_section_omp(&med, &dc, 4);
+            for (int l = 0; l < nbin * nq; l++) printf("dcs_data %d %d %.17g\n", d, l, dc.data[l]);
+            for (int l = 0; l < nbin; l++) printf("dcs_mean %d %d %.17g\n", d, l, dc.mean[l]);
+            for (int l = 0; l < nbin * nc; l++) printf("dcs_curve %d %d %.17g\n", d, l, dc.curve[l]);
+            free(dc.data);
+            free(dc.mean);
+            free(dc.curve);
             free(med.pos);
         } else {
             return 2;

@@ -168,6 +168,7 @@ def reference_runs():
     runs["cases"].extend(chistogram_cases(r))
     runs["cases"].extend(logcut_cases(r))
     runs["cases"].extend(wfcut_cases(r))
+    runs["cases"].extend(dcs_cases(r))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
@@ -259,6 +260,24 @@ def wfcut_cases(r):
     return out
 
 
+def dcs_cases(r):
+    """The differential cross section (run_differential_cross_section_omp,
+    ms_core.c:526-594) with the reference's own steps on one thread: the samples
+    per seed and angle, the quantiles, mean and curves, and the
+    [diff_cross_section] section save_diff_cross_section writes."""
+    out = []
+    for d, n, k, nseed, iseed, nbin, thmin, thmax, nq, nc in ((3, 50, 1.2, 5, 1, 7, 1.0, 180.0, 5, 2),
+                                                             (2, 40, 2.0, 4, 3, 6, 0.5, 170.0, 3, 1)):
+        title = f"dcs d={d}"
+        smp, data, mean, curve, text = r.diff_cross_section(d, n, k, nseed, iseed, nbin, thmin, thmax, nq, nc,
+                                                            title, 1.5)
+        out.append({"kind": "diff_cross_section", "d": d, "n": n, "k": k, "nseed": nseed, "iseed": iseed,
+                    "nbin": nbin, "thmin": thmin, "thmax": thmax, "nq": nq, "nc": nc, "title": title,
+                    "realtime": 1.5, "samples": smp.tolist(), "data": data.tolist(), "mean": mean.tolist(),
+                    "curve": curve.tolist(), "text": text})
+    return out
+
+
 if __name__ == "__main__":
     if "--chistogram-only" in sys.argv:
         # add or refresh only the mu-plane histogram cases of an existing reference_runs.json
@@ -269,8 +288,8 @@ if __name__ == "__main__":
         r = Reference()
         runs["cases"] = [c for c in runs["cases"] if c["kind"] not in ("chistogram", "imag_mu", "wavefunction_file",
                                                                        "logcut", "wfcut_stats",
-                                                                       "wavefunction_cut_file")
-                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r) + wfcut_cases(r)
+                                                                       "wavefunction_cut_file", "diff_cross_section")
+                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r) + wfcut_cases(r) + dcs_cases(r)
         with open(path, "w") as f:
             json.dump(runs, f, indent=0)
         sys.exit(0)

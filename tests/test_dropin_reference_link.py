@@ -18,7 +18,8 @@ ms_main.c linked against libmsgpu.so ahead of it.  The dynamic linker then binds
 the core's calls of the hot-path functions and of the task drivers defined and
 called inside ms_core.c (run_tracelog_omp, run_random_function_omp,
 run_chistogram_omp, run_imag_mu_histogram_omp, run_wave_function_omp,
-run_wave_function_cut_omp, find_eigenstates_serial_1/2/3, compute_eigenstates)
+run_wave_function_cut_omp, run_differential_cross_section_omp,
+find_eigenstates_serial_1/2/3, compute_eigenstates)
 to libmsgpu.so, and libmsgpu's weak references to the reference's histogram,
 eigenstate-list and cut-statistics functions back to the core.
 No GPU is needed: the programs print their usage without touching the device."""
@@ -38,7 +39,8 @@ HOT = ["build_ms_matrix", "build_dk_ms_matrix", "build_plane_wave", "tracelog_lu
        "total_cross_section"]
 CALLED = ["build_ms_matrix", "build_plane_wave", "tracelog_lu", "dk_log_det_ms", "total_cross_section"]
 DRIVERS = ["run_tracelog_omp", "run_random_function_omp", "run_chistogram_omp", "run_imag_mu_histogram_omp",
-           "run_wave_function_omp", "run_wave_function_cut_omp", "find_eigenstates_serial_1", "find_eigenstates_serial_2",
+           "run_wave_function_omp", "run_wave_function_cut_omp", "run_differential_cross_section_omp",
+           "find_eigenstates_serial_1", "find_eigenstates_serial_2",
            "find_eigenstates_serial_3", "compute_eigenstates"]
 BACK = ["fill_chist", "append_list_ihist", "normalize_ihist", "alloc_eigenstate_list", "check_eigenstate_list",
         "store_data_wfcut"]

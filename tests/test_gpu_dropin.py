@@ -148,6 +148,10 @@ def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
     lines.append(f"wave {d} {n} 1 3 {k.real!r} {k.imag!r} {nx} {ny} " + " ".join(repr(v) for v in dom))
     kc, nbin, xmin, xmax = 1.5 - 0.01j, 17, -8.0, 8.0
     lines.append(f"cut 3 60 2 3 {kc.real!r} {kc.imag!r} {nbin} {xmin!r} {xmax!r}")
+    dcs = [c for c in ref_runs["cases"] if c["kind"] == "diff_cross_section"]
+    for c in dcs:
+        lines.append(f"dcs {c['d']} {c['n']} {c['iseed']} {c['nseed']} {c['k']!r} {c['nbin']} {c['thmin']!r} "
+                     f"{c['thmax']!r} {c['nq']} {c['nc']}")
     out = subprocess.run([str(exe)], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stdout[-2000:] + out.stderr[-2000:]
     roots = {0: [], 1: [], 2: []}
@@ -175,6 +179,8 @@ def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
             wave[("cut", int(f[1]), int(f[2]))] = complex(float(f[3]), float(f[4]))
         elif f[0] == "cut_med_kept":
             wave["cut_med_kept"] = int(f[1])
+        elif f[0].startswith("dcs_"):
+            wave.setdefault((f[0], int(f[1])), {})[int(f[2])] = float(f[3])
     # determinant method: the reference's root set; Muller methods: the same list in the same order
     want = cplx(ab["roots"])
     assert nroot[0][0] == len(want) and nroot[0][1] > 0
@@ -214,3 +220,11 @@ def test_dropin_eigenstates_and_wave(ms, oracle, ref_runs, tmp_path):
         got = np.array([wave[("cut", s, i)] for i in range(nbin)])
         assert np.max(np.abs(got - want)) < 1e-10 * np.max(np.abs(want))
     assert wave["cut_med_kept"] == 1
+    # run_differential_cross_section_omp: the reference's quantiles, mean and curves
+    for c in dcs:
+        scale = np.max(np.array(c["samples"]))
+        for key, want in (("dcs_data", c["data"]), ("dcs_mean", c["mean"]), ("dcs_curve", c["curve"])):
+            w = np.array(want).reshape(-1)
+            got = wave[(key, c["d"])]
+            g = np.array([got[l] for l in range(w.size)])
+            assert np.max(np.abs(g - w)) < 1e-10 * scale, (key, c["d"])

@@ -107,3 +107,20 @@ def test_wave_cut_matches_oracle(ms, oracle, d, precision):
     for key, v in (("repsi", want.real), ("impsi", want.imag), ("density", np.abs(want) ** 2)):
         ref = np.array([_mean_quartiles(v[:, i]) for i in range(nbin)])
         assert np.max(np.abs(st[key] - ref)) < 1e-9 * np.max(np.abs(ref)), key
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_diff_cross_section_matches_reference(ms, ref_runs, precision):
+    """run_differential_cross_section_omp's samples (far-field amplitude of every
+    seed at every angle) against the reference's own run, relative to the largest
+    sample; then the statistics of the run_differential_cross_section path."""
+    for c in [c for c in ref_runs["cases"] if c["kind"] == "diff_cross_section"]:
+        media = [ms.Medium(c["d"], c["n"], seed=c["iseed"] + s) for s in range(c["nseed"])]
+        want = np.array(c["samples"])
+        got = ms.diff_cross_section(media, c["k"], c["nbin"], c["thmin"], c["thmax"], precision)
+        assert got.shape == want.shape
+        assert np.max(np.abs(got - want)) < 1e-10 * np.max(want), (c["d"], precision)
+        st = ms.run_differential_cross_section(media, c["k"], c["nbin"], c["thmin"], c["thmax"], c["nq"], c["nc"],
+                                               precision)
+        for key in ("data", "mean", "curve"):
+            assert np.max(np.abs(st[key] - np.array(c[key]))) < 1e-10 * np.max(want), key
