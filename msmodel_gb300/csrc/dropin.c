@@ -517,7 +517,8 @@ void run_differential_cross_section_omp(msgpu_ref_medium* med, msgpu_ref_dcs* dc
     for (int i = 0; i < nb; i++) {
         double* x = smp + (size_t)i * ns;
         qsort(x, (size_t)ns, sizeof(double), cmp_double);
-        for (int q = 0; q < dcs->nq; q++) dcs->data[q + i * dcs->nq] = quantile_sorted(ns, x, ((double)q) / (dcs->nq - 1));
+        for (int q = 0; q < dcs->nq; q++)
+            dcs->data[q + i * dcs->nq] = quantile_sorted(ns, x, ((double)q) / (dcs->nq - 1));
         double sum = 0.;
         for (int s = 0; s < ns; s++) sum += x[s];
         dcs->mean[i] = sum / ns;

@@ -134,12 +134,18 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
                                          int ny, const double* dom, double* function, double* density, double* psi,
                                          double* amps, int precision) {
     using namespace msg;
-    if (nmed < 1 || !media || nk < 1 || !ks || nx < 2 || ny < 2 || !dom || !function || !density) return MSGPU_E_ARG;
+    if (nmed < 1 || !media || nk < 1 || !ks || nx < 2 || ny < 2 || !dom || !function || !density)
+        return record_error(MSGPU_E_ARG,
+                            "wave_function: bad argument (nmed, nk >= 1; nx, ny >= 2; non-null pointers)");
     const int n = media[0].n, d = media[0].d;
     for (int m = 0; m < nmed; ++m)
-        if (media[m].n != n || media[m].d != d || !media[m].pos) return MSGPU_E_ARG;
+        if (media[m].n != n || media[m].d != d || !media[m].pos)
+            return record_error(MSGPU_E_ARG,
+                                "wave_function: every medium needs the same n and d, and positions");
     const size_t np = (size_t)nx * ny;
-    if (np > (size_t)1 << 31 || (size_t)nk > 65535) return MSGPU_E_SIZE;
+    if (np > (size_t)1 << 31 || (size_t)nk > 65535)
+        return record_error(MSGPU_E_SIZE,
+                            "wave_function: more than 2^31 pixels or 65535 wave numbers");
     // every (medium, k) solve in one job: item m * nk + kk
     const int nitem = nmed * nk;
     std::vector<double> iks(2 * (size_t)nitem), sig(2 * (size_t)nitem), a(2 * (size_t)nitem * n);
@@ -179,12 +185,12 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
         cudaMalloc(&dks, sizeof(double) * 2 * nk) || cudaMalloc(&dfun, sizeof(double) * plane) ||
         cudaMalloc(&dden, sizeof(double) * plane) || (psi && cudaMalloc(&dpsi, sizeof(double) * 2 * plane))) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "wave_function: device allocation failed");
     }
     if (cudaMemset(dfun, 0, sizeof(double) * plane) || cudaMemset(dden, 0, sizeof(double) * plane) ||
         cudaMemcpy(dks, ks, sizeof(double) * 2 * nk, cudaMemcpyHostToDevice)) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "wave_function: upload to the device failed");
     }
     GridArgs A;
     A.d = d;
@@ -206,7 +212,7 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
             cudaMemcpy(damp, a.data() + 2 * (size_t)m * nk * n, sizeof(double) * 2 * (size_t)nk * n,
                        cudaMemcpyHostToDevice)) {
             cleanup();
-            return MSGPU_E_CUDA;
+            return record_error(MSGPU_E_CUDA, "wave_function: upload to the device failed");
         }
         A.psi = m == 0 ? dpsi : nullptr;
         if (use_df) k_psi_grid_df3<<<grid, PT>>>(A);
@@ -214,14 +220,14 @@ extern "C" int msgpu_wave_function_batch(int nmed, const msgpu_medium* media, in
         count_launches(1);
         if (cudaGetLastError() != cudaSuccess) {
             cleanup();
-            return MSGPU_E_CUDA;
+            return record_error(MSGPU_E_CUDA, "wave_function: kernel launch failed");
         }
     }
     cudaError_t ce = cudaMemcpy(function, dfun, sizeof(double) * plane, cudaMemcpyDeviceToHost);
     if (ce == cudaSuccess) ce = cudaMemcpy(density, dden, sizeof(double) * plane, cudaMemcpyDeviceToHost);
     if (ce == cudaSuccess && psi) ce = cudaMemcpy(psi, dpsi, sizeof(double) * 2 * plane, cudaMemcpyDeviceToHost);
     cleanup();
-    if (ce != cudaSuccess) return MSGPU_E_CUDA;
+    if (ce != cudaSuccess) return record_error(MSGPU_E_CUDA, "wave_function: copy of the results to the host failed");
     // divide_wfun (wave_function_util.c:86): average over the realisations
     for (size_t l = 0; l < plane; ++l) {
         function[l] /= nmed;
@@ -248,11 +254,15 @@ extern "C" int msgpu_wave_function(int nmed, const msgpu_medium* media, const do
 extern "C" int msgpu_wave_cut(int nmed, const msgpu_medium* media, const double* k, int nbin, double xmin,
                               double xmax, double* psi, double* amps, int precision) {
     using namespace msg;
-    if (nmed < 1 || !media || !k || nbin < 2 || !psi) return MSGPU_E_ARG;
+    if (nmed < 1 || !media || !k || nbin < 2 || !psi)
+        return record_error(MSGPU_E_ARG,
+                            "wave_cut: bad argument (nmed >= 1, nbin >= 2, non-null pointers)");
     const int n = media[0].n, d = media[0].d;
     for (int m = 0; m < nmed; ++m)
-        if (media[m].n != n || media[m].d != d || !media[m].pos) return MSGPU_E_ARG;
-    if ((size_t)nmed * nbin > (size_t)1 << 31) return MSGPU_E_SIZE;
+        if (media[m].n != n || media[m].d != d || !media[m].pos)
+            return record_error(MSGPU_E_ARG,
+                                "wave_cut: every medium needs the same n and d, and positions");
+    if ((size_t)nmed * nbin > (size_t)1 << 31) return record_error(MSGPU_E_SIZE, "wave_cut: more than 2^31 samples");
     std::vector<double> iks(2 * (size_t)nmed), sig(2 * (size_t)nmed), a(2 * (size_t)nmed * n);
     std::vector<int> im(nmed), st(nmed);
     for (int m = 0; m < nmed; ++m) {
@@ -288,14 +298,14 @@ extern "C" int msgpu_wave_cut(int nmed, const msgpu_medium* media, const double*
         cudaMalloc(&dks, sizeof(double) * 2) || cudaMalloc(&dfun, sizeof(double) * nbin) ||
         cudaMalloc(&dden, sizeof(double) * nbin) || cudaMalloc(&dpsi, sizeof(double) * 2 * rows)) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "wave_cut: device allocation failed");
     }
     if (cudaMemcpy(dpos, pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice) ||
         cudaMemcpy(damp, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice) ||
         cudaMemcpy(dks, k, sizeof(double) * 2, cudaMemcpyHostToDevice) ||
         cudaMemset(dfun, 0, sizeof(double) * nbin) || cudaMemset(dden, 0, sizeof(double) * nbin)) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "wave_cut: upload to the device failed");
     }
     GridArgs A;
     A.d = d;
@@ -319,12 +329,12 @@ extern "C" int msgpu_wave_cut(int nmed, const msgpu_medium* media, const double*
         count_launches(1);
         if (cudaGetLastError() != cudaSuccess) {
             cleanup();
-            return MSGPU_E_CUDA;
+            return record_error(MSGPU_E_CUDA, "wave_cut: kernel launch failed");
         }
     }
     const cudaError_t ce = cudaMemcpy(psi, dpsi, sizeof(double) * 2 * rows, cudaMemcpyDeviceToHost);
     cleanup();
-    if (ce != cudaSuccess) return MSGPU_E_CUDA;
+    if (ce != cudaSuccess) return record_error(MSGPU_E_CUDA, "wave_cut: copy of the results to the host failed");
     int any = 0;
     for (int v : st) any |= v;
     return any;
@@ -388,11 +398,17 @@ extern "C" int msgpu_diff_cross_section(int nmed, const msgpu_medium* media, dou
                                         double thmax, double* samples, int precision) {
     using namespace msg;
     if (nmed < 1 || nmed > 65535 || !media || nbin < 2 || !samples || !(thmin > 0.0) || !(thmax > 0.0))
-        return MSGPU_E_ARG;
+        return record_error(MSGPU_E_ARG,
+                            "diff_cross_section: bad argument (1 <= nmed <= 65535, nbin >= 2, thmin and thmax > 0, "
+                            "non-null pointers)");
     const int n = media[0].n, d = media[0].d;
     for (int m = 0; m < nmed; ++m)
-        if (media[m].n != n || media[m].d != d || !media[m].pos) return MSGPU_E_ARG;
-    if ((size_t)nmed * nbin > (size_t)1 << 31) return MSGPU_E_SIZE;
+        if (media[m].n != n || media[m].d != d || !media[m].pos)
+            return record_error(MSGPU_E_ARG,
+                                "diff_cross_section: every medium needs the same n and d, and positions");
+    if ((size_t)nmed * nbin > (size_t)1 << 31)
+        return record_error(MSGPU_E_SIZE,
+                            "diff_cross_section: more than 2^31 samples");
     std::vector<double> iks(2 * (size_t)nmed), sig(2 * (size_t)nmed), a(2 * (size_t)nmed * n);
     std::vector<int> im(nmed), st(nmed);
     for (int m = 0; m < nmed; ++m) {
@@ -413,30 +429,33 @@ extern "C" int msgpu_diff_cross_section(int nmed, const msgpu_medium* media, dou
     }
     const double prefac = std::pow(k / (2 * pi), d - 3) / (16 * pi * pi);
     std::vector<double> pos((size_t)nmed * n * d);
-    for (int m = 0; m < nmed; ++m) std::copy(media[m].pos, media[m].pos + (size_t)n * d, pos.begin() + (size_t)m * n * d);
+    for (int m = 0; m < nmed; ++m)
+        std::copy(media[m].pos, media[m].pos + (size_t)n * d, pos.begin() + (size_t)m * n * d);
     double *dpos = nullptr, *damp = nullptr, *dcs = nullptr, *dout = nullptr;
     auto cleanup = [&]() { cudaFree(dpos); cudaFree(damp); cudaFree(dcs); cudaFree(dout); };
     const size_t nout = (size_t)nmed * nbin;
     if (cudaMalloc(&dpos, sizeof(double) * pos.size()) || cudaMalloc(&damp, sizeof(double) * a.size()) ||
         cudaMalloc(&dcs, sizeof(double) * cs.size()) || cudaMalloc(&dout, sizeof(double) * nout)) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "diff_cross_section: device allocation failed");
     }
     if (cudaMemcpy(dpos, pos.data(), sizeof(double) * pos.size(), cudaMemcpyHostToDevice) ||
         cudaMemcpy(damp, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice) ||
         cudaMemcpy(dcs, cs.data(), sizeof(double) * cs.size(), cudaMemcpyHostToDevice)) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "diff_cross_section: upload to the device failed");
     }
     k_far_field<<<dim3((unsigned)nbin, (unsigned)nmed), FF_NT>>>(d, n, nmed, k, dpos, damp, dcs, prefac, dout);
     count_launches(1);
     if (cudaGetLastError() != cudaSuccess) {
         cleanup();
-        return MSGPU_E_CUDA;
+        return record_error(MSGPU_E_CUDA, "diff_cross_section: kernel launch failed");
     }
     const cudaError_t ce = cudaMemcpy(samples, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost);
     cleanup();
-    if (ce != cudaSuccess) return MSGPU_E_CUDA;
+    if (ce != cudaSuccess)
+        return record_error(MSGPU_E_CUDA,
+                            "diff_cross_section: copy of the results to the host failed");
     int any = 0;
     for (int v : st) any |= v;
     return any;

@@ -122,3 +122,23 @@ def test_eigvals_entry_rejects_bad_arguments_without_a_gpu(libpath):
     assert L.msgpu_eigvals_batch_mtype(1, 1, api._media_array([big]), 1, im, ks, mu, st, None) == -4
     assert b"4097" in L.msgpu_last_error()
     assert L.msgpu_eigvals_batch_mtype(0, 0, api._media_array([small]), 1, im, ks, mu, st, None) == -1
+
+
+def test_wave_cut_and_dcs_entries_reject_bad_arguments_without_a_gpu(libpath):
+    """The cut and differential cross section entries check their arguments
+    before any device work and say why in msgpu_last_error."""
+    import msmodel_gb300 as ms
+    from msmodel_gb300 import api
+    L = ms.lib()
+    a = ms.Medium(3, 10, pos=np.zeros(30), seed=1)
+    b = ms.Medium(3, 11, pos=np.zeros(33), seed=1)
+    k = np.array([1.0, 0.0])
+    psi = np.zeros(2 * 2 * 8)
+    assert L.msgpu_wave_cut(1, api._media_array([a]), k, 1, -1.0, 1.0, psi, None, 0) == -1
+    assert b"nbin" in L.msgpu_last_error()
+    assert L.msgpu_wave_cut(2, api._media_array([a, b]), k, 8, -1.0, 1.0, psi, None, 0) == -1
+    assert b"same n" in L.msgpu_last_error()
+    out = np.zeros(2 * 8)
+    assert L.msgpu_diff_cross_section(1, api._media_array([a]), 1.0, 8, 0.0, 180.0, out, 0) == -1
+    assert b"thmin" in L.msgpu_last_error()
+    assert L.msgpu_diff_cross_section(70000, api._media_array([a]), 1.0, 8, 1.0, 180.0, out, 0) == -1
