@@ -16,6 +16,7 @@
 #include <complex>
 #include <vector>
 #include "msgpu.h"
+#include "error_text.h"
 
 namespace {
 
@@ -73,7 +74,8 @@ extern "C" int msgpu_solve_aberth_batch(int nmed, const msgpu_medium* media, con
                                         double* roots, int* nroots, int* nevals) {
     if (nmed < 1 || !media || !dom || nz < 0 || (nz > 0 && !z0) || nexpsup < 0 || nexpsup > 16 || maxit < 0 ||
         !roots || !nroots)
-        return MSGPU_E_ARG;
+        return msg::record_error(MSGPU_E_ARG, "solve_aberth_batch: bad argument (nmed >= 1, nz >= 0, nexpsup in "
+                                              "0..16, maxit >= 0, non-null pointers)");
     std::vector<Realisation> R(nmed);
     long long ne = 0;
     for (int r = 0; r < nmed; ++r) {

@@ -4,6 +4,7 @@
 #include <stddef.h>
 #include "msgpu.h"
 #include "cplx.cuh"
+#include "error_text.h"
 
 namespace msg {
 
@@ -36,8 +37,6 @@ struct EngineParams {
 
 // adds to the library's count of kernel launches (msgpu_launch_count)
 void count_launches(int n);
-// sets the text msgpu_last_error returns and passes `code` through
-int record_error(int code, const char* what);
 
 // Mixed-precision engine (mixed.cu).  Returns 0 when it ran the job, a
 // negative MSGPU_E* code on error.

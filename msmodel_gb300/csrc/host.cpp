@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdint>
 #include "msgpu.h"
+#include "error_text.h"
 
 namespace {
 
@@ -75,7 +76,8 @@ extern "C" {
 // fill_medium (src/core/medium_util.c:164-193) for the four shapes, then the
 // volume-preserving stretch of the first coordinate when ratio != 1.
 int msgpu_fill_medium(int d, int n, int shape, double ratio, uint64_t seed, double* pos) {
-    if (d < 1 || d > 20 || n < 1 || !pos || ratio < 1.0) return MSGPU_E_ARG;
+    if (d < 1 || d > 20 || n < 1 || !pos || ratio < 1.0)
+        return msg::record_error(MSGPU_E_ARG, "fill_medium: bad argument (d in 1..20, n >= 1, ratio >= 1, pos)");
     Ran rng(seed);
     if (d == 1 && shape == MSGPU_BALL) shape = MSGPU_CUBE;
     const int ntot = n * d;
@@ -117,7 +119,7 @@ int msgpu_fill_medium(int d, int n, int shape, double ratio, uint64_t seed, doub
         break;
     }
     default:
-        return MSGPU_E_ARG;
+        return msg::record_error(MSGPU_E_ARG, "fill_medium: unknown shape");
     }
     if (ratio != 1.0 && d != 1) {
         double f2 = std::pow(ratio, -1.0 / d), f1 = ratio * f2;

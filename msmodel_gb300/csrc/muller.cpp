@@ -29,6 +29,7 @@
 #include <complex>
 #include <vector>
 #include "msgpu.h"
+#include "error_text.h"
 
 namespace {
 
@@ -57,7 +58,8 @@ extern "C" int msgpu_find_roots_muller_batch(int method, int nmed, const msgpu_m
                                              double* roots, int* nroots, int* nevals) {
     if ((method != MSGPU_EIG_MINEIGVAL && method != MSGPU_EIG_INVTRACEINV) || nmed < 1 || !media || !dom || nz < 0 ||
         (nz > 0 && !z0) || !roots || !nroots)
-        return MSGPU_E_ARG;
+        return msg::record_error(MSGPU_E_ARG, "find_roots_muller_batch: bad argument (method mineigval or "
+                                              "invtraceinv, nmed >= 1, nz >= 0, non-null pointers)");
     // find_root_muller refuses these parameters (root_finder.c:344-347): no root converges
     const bool refused = maxit <= 1 || !(toler > 0.0);
     const double DELTA = 1e-4;  // finite-difference step of root_finder.c:19

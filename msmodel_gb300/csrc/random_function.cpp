@@ -13,13 +13,15 @@
 #include <cmath>
 #include <vector>
 #include "msgpu.h"
+#include "error_text.h"
 
 extern "C" int msgpu_random_function(int type, int d, int n, int shape, double ratio, const msgpu_model* model,
                                      int nseed, int nbin, double xmin, double xmax, double* data, int* status,
                                      int precision) {
     if ((type != MSGPU_RF_CRSEC && type != MSGPU_RF_DOS) || d < 1 || n < 1 || !model || nseed < 1 || nbin < 2 ||
         !(xmin > 0.0) || !(xmax > 0.0) || !data)
-        return MSGPU_E_ARG;
+        return msg::record_error(MSGPU_E_ARG, "random_function: bad argument (type crsec or dos, d, n, nseed >= 1, "
+                                              "nbin >= 2, xmin and xmax > 0, non-null pointers)");
     std::vector<double> pos((size_t)nseed * n * d);
     std::vector<msgpu_medium> media(nseed);
     for (int g = 0; g < nseed; ++g) {

@@ -142,3 +142,34 @@ def test_wave_cut_and_dcs_entries_reject_bad_arguments_without_a_gpu(libpath):
     assert L.msgpu_diff_cross_section(1, api._media_array([a]), 1.0, 8, 0.0, 180.0, out, 0) == -1
     assert b"thmin" in L.msgpu_last_error()
     assert L.msgpu_diff_cross_section(70000, api._media_array([a]), 1.0, 8, 1.0, 180.0, out, 0) == -1
+
+
+def test_host_entries_say_why_they_reject_arguments(libpath):
+    """fill_medium, the two root searches and the random function check their
+    arguments on the host and set msgpu_last_error before returning MSGPU_E_ARG."""
+    import ctypes as C
+    import msmodel_gb300 as ms
+    from msmodel_gb300 import api
+    L = ms.lib()
+    pos = np.zeros(30)
+    assert L.msgpu_fill_medium(0, 10, 1, 1.0, 1, pos) == -1
+    assert b"fill_medium" in L.msgpu_last_error()
+    assert L.msgpu_fill_medium(3, 10, 9, 1.0, 1, pos) == -1
+    assert b"shape" in L.msgpu_last_error()
+    a = ms.Medium(3, 10, pos=pos, seed=1)
+    dom = np.array([0.5, 3.0, -1.0, 0.0])
+    z0 = np.array([1.0, -0.5, 2.0, -0.5])
+    roots = np.zeros(4)
+    nr = np.zeros(1, dtype=np.int32)
+    ne = C.c_int(0)
+    assert L.msgpu_solve_aberth_batch(1, api._media_array([a]), dom, 2, z0, 17, 30, 1e-10, 0, roots, nr,
+                                      C.byref(ne)) == -1
+    assert b"nexpsup" in L.msgpu_last_error()
+    assert L.msgpu_find_roots_muller_batch(5, 1, api._media_array([a]), dom, 2, z0, 30, 1e-10, 0, roots, nr,
+                                           C.byref(ne)) == -1
+    assert b"method" in L.msgpu_last_error()
+    m = api._model()
+    data = np.zeros(8)
+    assert L.msgpu_random_function(4, 3, 10, 1, 1.0, C.byref(m), 2, 4, 0.5, 2.5, data, np.zeros(8, dtype=np.int32),
+                                   0) == -1
+    assert b"random_function" in L.msgpu_last_error()
