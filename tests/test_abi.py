@@ -38,11 +38,14 @@ def test_exports_every_declared_symbol(libpath):
     assert not missing, missing
 
 
-def test_dropin_c_program_links(libpath, tmp_path):
-    exe = tmp_path / "dropin_check"
-    src = os.path.join(ROOT, "tests", "dropin_check.c")
-    r = subprocess.run(["gcc", "-O1", "-std=gnu11", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
-                        libpath, "-Wl,-rpath," + os.path.dirname(libpath), "-lm"], capture_output=True, text=True)
+@pytest.mark.parametrize("prog", ["dropin_check", "dropin_roots_check"])
+def test_dropin_c_program_links(libpath, tmp_path, prog):
+    """The C callers of the drop-ins compile warning-free against the headers and link."""
+    exe = tmp_path / prog
+    src = os.path.join(ROOT, "tests", prog + ".c")
+    r = subprocess.run(["gcc", "-O1", "-std=gnu11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src,
+                        "-o", str(exe), libpath, "-Wl,-rpath," + os.path.dirname(libpath), "-lm"],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
 
