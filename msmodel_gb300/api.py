@@ -535,7 +535,7 @@ def diff_cross_section(media, k, nbin, thmin, thmax, precision="fp64"):
 
 def dcs_statistics(samples, nq, nc):
     """The statistics run_differential_cross_section_omp forms from samples[nbin,
-    nseed] (ms_core.c:568-583): curve[i, s] the first nc seeds' samples, then per
+    nseed] (ms_core.c:572-583): curve[i, s] the first nc seeds' samples, then per
     bin the samples sorted, data[i, q] their quantile at q/(nq-1) and mean[i]."""
     samples = np.asarray(samples, dtype=np.float64)
     nbin = samples.shape[0]

@@ -454,7 +454,7 @@ void run_wave_function_cut_omp(msgpu_ref_medium* med, msgpu_ref_wfcut* wc, int n
     if (st & (MSGPU_S_SINGULAR | MSGPU_S_NONFINITE))
         printf("[WARN] run_wave_function_cut_omp: a singular or non-finite solve reached the samples (status %d).\n",
                st);
-    for (int s = 0; s < ns; s++)  /* bin-major samples, [s + i*nseed] (ms_core.c:687-689) */
+    for (int s = 0; s < ns; s++)  /* bin-major samples, [s + i*nseed] (ms_core.c:690-692) */
         for (int i = 0; i < nb; i++) {
             const double a = psi[2 * ((size_t)s * nb + i)], b = psi[2 * ((size_t)s * nb + i) + 1];
             re[s + (size_t)i * ns] = a;
@@ -509,7 +509,7 @@ void run_differential_cross_section_omp(msgpu_ref_medium* med, msgpu_ref_dcs* dc
     if (st & (MSGPU_S_SINGULAR | MSGPU_S_NONFINITE))
         printf("[WARN] run_differential_cross_section_omp: a singular or non-finite solve reached the samples "
                "(status %d).\n", st);
-    /* ms_core.c:568-583: sample curves of the first nc seeds (at most nseed of them:
+    /* ms_core.c:572-583: sample curves of the first nc seeds (at most nseed of them:
      * the reference's loop reads past its samples beyond that), then per bin the
      * sorted samples' quantiles and mean */
     for (int s = 0; s < dcs->nc && s < ns; s++)

@@ -344,7 +344,7 @@ namespace msg {
 
 constexpr int FF_NT = 128;
 
-// Far-field amplitude of run_differential_cross_section_omp (ms_core.c:556-560):
+// Far-field amplitude of run_differential_cross_section_omp (ms_core.c:556-562):
 // for medium m = blockIdx.y and angle i = blockIdx.x, atot = sum_j conj(b_j) a_j
 // with b_j = exp(i k (cos th x_j + sin th y_j)) (build_plane_wave,
 // ms_matrix_util.c:88-107; d = 1: exp(i k sign(cos th) x_j)) and real k, so

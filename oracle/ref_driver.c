@@ -434,7 +434,7 @@ void ref_logcut(int ns, double rek, double imkmin, double imkmax, int nseed, con
 /* store_data_wfcut (wave_function_cut_util.c:92-114) on bin-major samples
  * [s + i*nseed] of Re psi, Im psi and |psi|^2: out_*[3*i..3*i+2] = mean and
  * the first and third quartiles of bin i, the reference's own statistics of
- * run_wave_function_cut_omp (ms_core.c:695). */
+ * run_wave_function_cut_omp (ms_core.c:701). */
 void ref_wfcut_stats(int nseed, int nbin, const double* re, const double* im, const double* den, double* out_re,
                      double* out_im, double* out_den) {
     WaveFunctionCut wc;

@@ -240,7 +240,7 @@ def logcut_cases(r):
 
 def wfcut_cases(r):
     """The wavefunction cut's statistics (store_data_wfcut, wave_function_cut_util.c:92-114,
-    called by run_wave_function_cut_omp, ms_core.c:695): mean and quartiles per bin of
+    called by run_wave_function_cut_omp, ms_core.c:701): mean and quartiles per bin of
     seeded psi samples, including one seed, two seeds and tied samples."""
     rng = np.random.default_rng(11)
     out = []
