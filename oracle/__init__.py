@@ -83,6 +83,8 @@ class Oracle:
         L.orc_halton_points.argtypes = [_dp, C.c_int, _dp]
         L.orc_solve_aberth.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, C.c_int, _dp, C.c_int,
                                        C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)]
+        L.orc_psi_grid.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int]
+        L.orc_psi_grid.restype = None
         L.orc_wavefunction.argtypes = [C.c_int, C.c_int, _dp, C.POINTER(_Model), _dp, C.c_int, C.c_int, _dp, _dp,
                                        _dp, C.c_int, C.c_int]
         self.use_lapack = 0
@@ -214,6 +216,16 @@ class Oracle:
                                 np.asarray(dom, dtype=np.float64), amp, psi, nthreads or os.cpu_count(),
                                 self.use_lapack)
         return amp.view(np.complex128).copy(), psi.view(np.complex128).copy()
+
+
+    def psi_grid(self, d, n, pos, k, nx, ny, dom, amp, nthreads=None):
+        """psi on the nx x ny grid of dom for given amplitudes amp (the grid part of
+        wavefunction, without the solve)."""
+        psi = np.zeros(2 * nx * ny)
+        a = np.ascontiguousarray(np.asarray(amp, dtype=np.complex128)).view(np.float64)
+        self.L.orc_psi_grid(d, n, np.ascontiguousarray(pos, dtype=np.float64), _c2(k), nx, ny,
+                            np.asarray(dom, dtype=np.float64), a, psi, nthreads or os.cpu_count())
+        return psi.view(np.complex128).copy()
 
 
 class Reference:

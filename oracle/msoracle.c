@@ -695,6 +695,16 @@ int orc_wavefunction(int d, int n, const double* pos, const orc_model* m, const 
     build_m(d, n, pos, m, k, a);
     int info = orc_solve(n, (double*)a, (double*)ph, use_lapack);
     free(a);
+    orc_psi_grid(d, n, pos, kk, nx, ny, dom, amp, psi, nthreads);
+    return info;
+}
+
+/* eval_total_wave (incident_wave_util.c:87-96) at every pixel of the grid
+ * (get_pos_wfun, wave_function_util.c:76-81) for given amplitudes amp */
+void orc_psi_grid(int d, int n, const double* pos, const double* kk, int nx, int ny, const double* dom,
+                  const double* amp, double* psi, int nthreads) {
+    cplx k = ld2(kk);
+    const cplx* ph = (const cplx*)amp;
     double dx = (dom[1] - dom[0]) / (nx - 1), dy = (dom[3] - dom[2]) / (ny - 1);
 #pragma omp parallel for schedule(static, 1) num_threads(nthreads)
     for (int l = 0; l < nx * ny; l++) {
@@ -705,5 +715,4 @@ int orc_wavefunction(int d, int n, const double* pos, const orc_model* m, const 
         for (int i = 0; i < n; i++) s += ph[i] * free_green(d, k, dist(d, pos + i * d, r));
         st2(psi + 2 * l, s + cexp(I * k * r[0]));
     }
-    return info;
 }

@@ -81,6 +81,8 @@ int orc_solve_aberth(int d, int n, const double* pos, const orc_model* m, const 
                      int* nevals);
 
 /* plane-wave (+x) wavefunction: a = M^-1 phi, psi on an nx*ny grid of (x,y,0) */
+void orc_psi_grid(int d, int n, const double* pos, const double* k, int nx, int ny, const double* dom,
+                  const double* amp, double* psi, int nthreads);
 int orc_wavefunction(int d, int n, const double* pos, const orc_model* m, const double* k,
                      int nx, int ny, const double* dom, double* amp, double* psi, int nthreads,
                      int use_lapack);
