@@ -2,7 +2,7 @@
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
 ``--impl reference`` legs of ``bench.py`` import this package, and only as
-the checker or the timed CPU baseline.  The product (``msmodel_gb300``)
+the reference results to compare with or the timed CPU baseline.  The product (``msmodel_gb300``)
 never imports it.
 
 ``Oracle`` wraps ``liboracle.so`` (the C restatement, ``msoracle.c``);

@@ -1,6 +1,6 @@
 """Every struct msgpu_dropin.h mirrors has the reference's layout: a C unit
 that includes the reference's own type headers (MSMODEL_REF, default
-/root/reference; absent on GPU machines, where this test skips) next to
+/root/reference; where the tree is absent this test skips) next to
 msgpu_dropin.h must compile with a static assertion on the size of each pair
 and on the offset of every field.  No GPU needed."""
 import os

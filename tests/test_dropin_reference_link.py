@@ -1,7 +1,7 @@
 """The function-level drop-in inside the reference's own build.
 
 Where the reference tree is present (MSMODEL_REF, default /root/reference;
-absent on GPU machines, where this test skips), compile every translation unit
+where the tree is absent this test skips), compile every translation unit
 of its src/core plus src/main/ms_main.c with the reference's own flags
 (Makefile:28-31: -fms-extensions -fopenmp), ms_matrix_util.c with the -D
 renames of the integration recipe, and link the result against libmsgpu.so and
