@@ -73,7 +73,7 @@ msgpu_dcomplex tracelog_lu(int n, msgpu_dcomplex* matrix) {
     int e = msgpu_tracelog_matrix(n, (const double*)matrix, out, &info);
     if (e) fail("tracelog_lu", e);
     if (info > 0) printf("[LAPACK] Element U(%d,%d) is exactly zero, the determinant will be singular.\n", info, info);
-    return out[0] + I * out[1];
+    return CMPLX(out[0], out[1]);
 }
 
 msgpu_dcomplex dk_log_det_ms(msgpu_ref_medium* med, msgpu_dcomplex k) {
@@ -83,7 +83,7 @@ msgpu_dcomplex dk_log_det_ms(msgpu_ref_medium* med, msgpu_dcomplex k) {
     int e = msgpu_dk_log_det_batch(1, &m, 1, NULL, kk, out, &st, MSGPU_FP64);
     if (e) fail("dk_log_det_ms", e);
     if (st & MSGPU_S_SINGULAR) printf("[LAPACK] Element U(i,i) is exactly zero, the inverse matrix will be singular.\n");
-    return out[0] + I * out[1];
+    return CMPLX(out[0], out[1]);
 }
 
 double total_cross_section(msgpu_ref_medium* med, double k) {
@@ -137,7 +137,7 @@ void run_tracelog_omp(msgpu_ref_medium* med, msgpu_ref_cdata* cdata, int nthread
     for (int s = 1; s <= nseed; s++)
         for (int l = 0; l < ntot; l++) {
             size_t it = (size_t)(s - 1) * ntot + l;
-            msgpu_dcomplex t = out[2 * it] + I * out[2 * it + 1];
+            msgpu_dcomplex t = CMPLX(out[2 * it], out[2 * it + 1]);
             cdata->data[l] = ((s - 1) * cdata->data[l] + t) / s;
         }
     /* leave the medium filled with the last seed, as the reference loop does */
@@ -352,7 +352,7 @@ static void find_roots(int method, msgpu_ref_eigls* eigls, int* nroot, msgpu_dco
                                           &nr, NULL);
     if (e) fail(method == 0 ? "find_eigenstates_serial_1" : method == 1 ? "find_eigenstates_serial_2"
                                                                         : "find_eigenstates_serial_3", e);
-    for (int i = 0; i < nr; i++) kroot[i] = roots[2 * i] + I * roots[2 * i + 1];
+    for (int i = 0; i < nr; i++) kroot[i] = CMPLX(roots[2 * i], roots[2 * i + 1]);
     *nroot = nr;
     if (method != 0)  /* the split into duplicates and failures is not kept */
         printf("[INFO] Found %d/%d valid roots, %d duplicates or failed.\n", nr, eigls->ntarget, nz - nr);
@@ -405,7 +405,7 @@ void compute_eigenstates(msgpu_ref_eigls* eigls, int nroot, msgpu_dcomplex* kroo
         for (int i = 0; i < ns; i++) {
             msgpu_ref_eigenstate* es = eigls->eigtab[i];
             es->kroot = kroot[i];
-            es->mu = lam[2 * i] + I * lam[2 * i + 1];
+            es->mu = CMPLX(lam[2 * i], lam[2 * i + 1]);
             memcpy(es->eigv, vec + 2 * (size_t)i * n, sizeof(double) * 2 * (size_t)n);
             if (st[i] & MSGPU_S_SINGULAR)  /* inverse_iteration's warning, ms_matrix_util.c:284 */
                 printf("[LAPACK] Element U(i,i) is exactly zero, the inverse power iteration will fail.\n");

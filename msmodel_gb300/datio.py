@@ -26,7 +26,8 @@ appends the section it names with the same keys, order and number formats:
 
 `parse_cdata` reads a data= line back (parse_complex_data,
 src/core/complex_vector_util.c:215-231).  Numbers go through C-style printf
-conversions (%g, %.16g, %+.16g), which Python's % operator reproduces.
+conversions (%g, %.16g, %+.16g), which Python's % operator reproduces except
+for the sign glibc writes on a NaN ("-nan", "+nan"), which _gfmt adds.
 """
 import math
 
@@ -40,10 +41,25 @@ MODEL_NAMES = ("hardsphere", "softsphere", "resonant", "maximum")
 SHAPE_NAMES = ("cube", "ball", "lattice", "gaussian")
 
 
+def _gfmt(v, prec=16, plus=False):
+    """%.<prec>g (or %+.<prec>g) as glibc's printf writes it: Python drops a
+    NaN's sign, glibc writes it ("-nan", and "+nan" under the plus flag)."""
+    v = float(v)
+    if v != v:
+        return "-nan" if math.copysign(1.0, v) < 0 else ("+nan" if plus else "nan")
+    return ("%+.*g" if plus else "%.*g") % (prec, v)
+
+
+def _cfmt(z, prec=16):
+    """A complex value as "%.<prec>g%+.<prec>gi" (save_cdata, save_eigenstate)."""
+    z = complex(z)
+    return _gfmt(z.real, prec) + _gfmt(z.imag, prec, True) + "i"
+
+
 def format_cdata(data):
     """The data= line of save_cdata: every value as "%.16lg%+.16lgi " then a newline."""
     z = np.asarray(data, dtype=np.complex128).reshape(-1)
-    return "data=" + "".join("%.16g%+.16gi " % (v.real, v.imag) for v in z) + "\n"
+    return "data=" + "".join(_cfmt(v) + " " for v in z) + "\n"
 
 
 def parse_cdata(line, n=None):
@@ -64,10 +80,7 @@ def parse_cdata(line, n=None):
 
 def _g16(v):
     """%.16g as glibc's printf writes it, NaN with its sign ("-nan") included."""
-    v = float(v)
-    if v != v:
-        return "-nan" if math.copysign(1.0, v) < 0 else "nan"
-    return "%.16g" % v
+    return _gfmt(v)
 
 
 def _append(fname, text):
@@ -95,8 +108,8 @@ def save_complexmap(fname, data, nx, ny, xrange, yrange, title="", realtime=0.0,
 def save_complexcut(fname, data, ns, kmin, kmax, title="", realtime=0.0, nseed=1):
     """A [kcut] section; data in get_arg_ccut order (3 (ns+2) values)."""
     kmin, kmax = complex(kmin), complex(kmax)
-    text = ("[kcut]\ntitle=%s\nrealtime=%g\nnseed=%d\nsample=%d\nkmin=%.12g%+.12gi\nkmax=%.12g%+.12gi\n"
-            % (title, realtime, nseed, ns, kmin.real, kmin.imag, kmax.real, kmax.imag))
+    text = ("[kcut]\ntitle=%s\nrealtime=%g\nnseed=%d\nsample=%d\nkmin=%s\nkmax=%s\n"
+            % (title, realtime, nseed, ns, _cfmt(kmin, 12), _cfmt(kmax, 12)))
     _append(fname, text + format_cdata(data) + "\n")
 
 
@@ -113,7 +126,7 @@ def save_random_function(fname, kind, data, xmin, xmax, title="", realtime=0.0):
     nbin, nseed = data.shape
     text = ("[random_function]\ntitle=%s\ntype=%s\nnseed=%d\nnbin=%d\nxmin=%.16g\nxmax=%.16g\nrealtime=%.16g\n"
             % (title, kind, nseed, nbin, xmin, xmax, realtime))
-    text += "data=" + "".join("%.16g " % v for v in data.reshape(-1)) + "\n\n"
+    text += "data=" + "".join(_g16(v) + " " for v in data.reshape(-1)) + "\n\n"
     _append(fname, text)
 
 
@@ -126,9 +139,9 @@ def save_eigenstate_list(fname, states, seed, method, ntarget, dom, maxit, toler
     text += "maxit=%d\ntoler=%g\nverb=%d\nrealtime=%g\n" % (maxit, toler, verb, realtime)
     for i, (k, mu, v) in enumerate(states):
         k, mu = complex(k), complex(mu)
-        text += "st%d_kroot=%.16g%+.16gi\n" % (i, k.real, k.imag)
-        text += "st%d_mu=%.16g%+.16gi\n" % (i, mu.real, mu.imag)
-        text += "st%d_eigv=" % i + "".join("%.16g%+.16gi " % (z.real, z.imag) for z in np.asarray(v)) + "\n"
+        text += "st%d_kroot=%s\n" % (i, _cfmt(k))
+        text += "st%d_mu=%s\n" % (i, _cfmt(mu))
+        text += "st%d_eigv=" % i + "".join(_cfmt(z) + " " for z in np.asarray(v)) + "\n"
     _append(fname, text + "\n")
 
 
@@ -141,13 +154,13 @@ def save_muplane(fname, hist, k, nseed, mtype="msmatrix", title="", color=("magm
     k = complex(k)
     xmin, xmax, ymin, ymax = hist["dom"]
     name, ctype, ctr, rev = color
-    text = "[muplane]\ntitle=%s\nmtype=%s\nk=%.16g%+.16gi\nnseed=%d\n" % (title, mtype, k.real, k.imag, nseed)
+    text = "[muplane]\ntitle=%s\nmtype=%s\nk=%s\nnseed=%d\n" % (title, mtype, _cfmt(k), nseed)
     data = np.asarray(hist["data"]).reshape(-1)
     ybin, xbin = np.asarray(hist["data"]).shape
     text += "xbin=%d\nybin=%d\n" % (xbin, ybin)
     text += "xrange=%.16g:%.16g\nyrange=%.16g:%.16g\n" % (xmin, xmax, ymin, ymax)
     avg, sig = complex(hist["avg"]), complex(hist["sigma"])
-    text += "avgz=%.16g%+.16gi\nsigmaz=%.16g%+.16gi\n" % (avg.real, avg.imag, sig.real, sig.imag)
+    text += "avgz=%s\nsigmaz=%s\n" % (_cfmt(avg), _cfmt(sig))
     text += "realtime=%g\ncolor=%s %s %g%s\n" % (realtime, name, ctype, ctr, " rev" if rev else "")
     text += "data=" + "".join(_g16(v) + " " for v in data) + "\n"
     mdata = np.asarray(hist["mdata"])

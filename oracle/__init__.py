@@ -270,6 +270,14 @@ class Reference:
         L.ref_diff_cross_section.argtypes = med[:-1] + [C.c_double, C.c_int, C.c_ulong, C.c_int, C.c_double,
                                                         C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_double,
                                                         C.c_char_p, _dp, _dp, _dp, _dp]
+        L.ref_save_medium.argtypes = med[:-1] + [C.c_char_p]
+        L.ref_save_kcut.argtypes = [C.c_int, _dp, _dp, C.c_int, C.c_char_p, C.c_double, _dp, C.c_char_p]
+        L.ref_save_kplane.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                      C.c_char_p, C.c_double, C.c_char_p, _dp, C.c_char_p]
+        L.ref_save_rfun.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_char_p, C.c_double, _dp,
+                                    C.c_char_p]
+        L.ref_save_eigls.argtypes = [C.c_int, C.c_int, C.c_ulong, C.c_int, C.c_int, _dp, C.c_int, C.c_double, C.c_int,
+                                     C.c_double, C.c_int, _dp, _dp, _dp, C.c_char_p]
         L.ref_wfcut_stats.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_random_function.argtypes = [C.c_int] + med[:-1] + [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
 
@@ -439,6 +447,42 @@ class Reference:
             with open(fname) as f:
                 text = f.read()
         return smp.reshape(nbin, nseed), data.reshape(nbin, nq), mean, curve.reshape(nbin, nc), text
+
+    @staticmethod
+    def _section(call):
+        """The text a reference writer appends to a fresh file."""
+        import tempfile
+        with tempfile.TemporaryDirectory() as tmp:
+            fname = os.path.join(tmp, "section.dat")
+            call(fname.encode())
+            with open(fname) as f:
+                return f.read()
+
+    def save_medium(self, d, n, model="maximum", params=(), shape="ball", ratio=1.0):
+        return self._section(lambda f: self.L.ref_save_medium(*self._med(d, n, model, params, shape, ratio, 1)[:-1],
+                                                              f))
+
+    def save_kcut(self, ns, zmin, zmax, nseed, title, realtime, data):
+        z = _cplx_array(data)
+        return self._section(lambda f: self.L.ref_save_kcut(ns, _c2(zmin), _c2(zmax), nseed, title.encode(),
+                                                            realtime, z, f))
+
+    def save_kplane(self, nx, ny, xmin, xmax, ymin, ymax, nseed, title, realtime, color, data):
+        z = _cplx_array(data)
+        return self._section(lambda f: self.L.ref_save_kplane(nx, ny, xmin, xmax, ymin, ymax, nseed, title.encode(),
+                                                              realtime, color.encode(), z, f))
+
+    def save_rfun(self, kind, nseed, nbin, xmin, xmax, title, realtime, data):
+        v = np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1))
+        return self._section(lambda f: self.L.ref_save_rfun({"crsec": 0, "dos": 1}[kind], nseed, nbin, xmin, xmax,
+                                                            title.encode(), realtime, v, f))
+
+    def save_eigls(self, d, n, seed, method, ntarget, dom, maxit, toler, verb, realtime, kroot, mu, eigv):
+        kr, m, ev = _cplx_array(kroot), _cplx_array(mu), _cplx_array(np.asarray(eigv).reshape(-1))
+        meth = {"determinant": 0, "mineigval": 1, "invtraceinv": 2}[method]
+        return self._section(lambda f: self.L.ref_save_eigls(d, n, seed, meth, ntarget,
+                                                             np.asarray(dom, dtype=np.float64), maxit, toler, verb,
+                                                             realtime, len(kr) // 2, kr, m, ev, f))
 
     def wfcut_stats(self, psi):
         """store_data_wfcut on psi[nseed, nbin]: (repsi, impsi, density) rows

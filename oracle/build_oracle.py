@@ -32,6 +32,9 @@ REF_SOURCES = [
     "wave_function_cut_util.c",
     # the differential cross section's angles and writer
     "diff_cross_section_util.c",
+    # the writers of the map, cut, random function and eigenstate list sections
+    "complex_map_util.c", "complex_cut_util.c", "random_function_util.c", "eigenstate_list_util.c",
+    "eigenstate_util.c", "square_well_resonances.c",
 ]
 
 

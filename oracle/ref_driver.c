@@ -34,6 +34,15 @@
 #include "wave_function_cut_util.h"
 #include "diff_cross_section_type.h"
 #include "diff_cross_section_util.h"
+#include "complex_map_type.h"
+#include "complex_map_util.h"
+#include "complex_cut_type.h"
+#include "complex_cut_util.h"
+#include "random_function_type.h"
+#include "random_function_util.h"
+#include "eigenstate_list_type.h"
+#include "eigenstate_list_util.h"
+#include "eigenstate_util.h"
 
 void zgesv_(int* n, int* nrhs, dcomplex* a, int* lda, int* ipiv, dcomplex* b, int* ldb, int* info);
 
@@ -528,5 +537,78 @@ void ref_diff_cross_section(int d, int n, int mtype, int np, const double* p, in
     memcpy(curve, dcs.curve, sizeof(double) * (size_t)nbin * nc);
     free(smp); free(m); free(a); free(b); free(ipiv);
     del_diff_cross_section(&dcs);
+    drop_medium(&med);
+}
+
+/* The reference's writers of the [medium], [kcut], [kplane], [random_function]
+ * and [eigenstate_list] sections (medium_util.c:420, complex_cut_util.c:106,
+ * complex_map_util.c:236, random_function_util.c:178,
+ * eigenstate_list_util.c:296) on structs its own init functions set up, with
+ * the given data; each appends its section to fname. */
+void ref_save_medium(int d, int n, int mtype, int np, const double* p, int shape, double ratio, const char* fname) {
+    Medium med;
+    make_medium(&med, d, n, mtype, np, p, shape, ratio, 1);
+    save_medium(&med, fname);
+    drop_medium(&med);
+}
+
+void ref_save_kcut(int ns, const double* zmin, const double* zmax, int nseed, const char* title, double realtime,
+                   const double* data, const char* fname) {
+    ComplexCut cc;
+    memset(&cc, 0, sizeof(cc));
+    init_complexcut(&cc, ns, zmin[0] + I * zmin[1], zmax[0] + I * zmax[1], nseed, title);
+    memcpy(cc.data, data, sizeof(dcomplex) * (size_t)cc.ntot);
+    cc.realtime = realtime;
+    save_complexcut(&cc, fname);
+    del_complexcut(&cc);
+}
+
+void ref_save_kplane(int nx, int ny, double xmin, double xmax, double ymin, double ymax, int nseed, const char* title,
+                     double realtime, const char* color, const double* data, const char* fname) {
+    ComplexMap cm;
+    memset(&cm, 0, sizeof(cm));
+    init_complexmap(&cm, nx, ny, xmin, xmax, ymin, ymax, nseed, title);
+    char a[128];
+    strncpy(a, color, sizeof(a) - 1);
+    a[sizeof(a) - 1] = '\0';
+    parse_colorrule(cm.colrule, a);
+    memcpy(cm.data, data, sizeof(dcomplex) * (size_t)cm.ntot);
+    cm.realtime = realtime;
+    save_complexmap(&cm, fname);
+    del_complexmap(&cm);
+}
+
+void ref_save_rfun(int type, int nseed, int nbin, double xmin, double xmax, const char* title, double realtime,
+                   const double* data, const char* fname) {
+    RandomFunction rf;
+    memset(&rf, 0, sizeof(rf));
+    char t[80];
+    strncpy(t, title, sizeof(t) - 1);
+    t[sizeof(t) - 1] = '\0';
+    init_random_function(&rf, (RandomFunctionType)type, nseed, nbin, xmin, xmax, t);
+    memcpy(rf.data, data, sizeof(double) * (size_t)rf.ntot);
+    rf.realtime = realtime;
+    save_random_function(&rf, fname);
+    del_random_function(&rf);
+}
+
+void ref_save_eigls(int d, int n, unsigned long seed, int method, int ntarget, const double* dom, int maxit,
+                    double toler, int verb, double realtime, int nstate, const double* kroot, const double* mu,
+                    const double* eigv, const char* fname) {
+    Medium med;
+    make_medium(&med, d, n, 3, 0, NULL, 1, 1.0, seed);
+    Domain dm = {dom[0], dom[1], dom[2], dom[3]};
+    EigenstateList el;
+    memset(&el, 0, sizeof(el));
+    init_eigenstate_list(&el, &med, seed, (EigenstateMethod)method, ntarget, &dm, maxit, toler, verb);
+    alloc_eigenstate_list(&el, nstate);
+    for (int i = 0; i < nstate; i++) {
+        el.eigtab[i]->kroot = CMPLX(kroot[2 * i], kroot[2 * i + 1]);
+        el.eigtab[i]->mu = CMPLX(mu[2 * i], mu[2 * i + 1]);
+        memcpy(el.eigtab[i]->eigv, eigv + 2 * (size_t)i * n, sizeof(dcomplex) * (size_t)n);
+    }
+    el.realtime = realtime;
+    save_eigenstate_list(&el, fname);
+    del_eigenstate_list(&el);
     drop_medium(&med);
 }

@@ -169,6 +169,7 @@ def reference_runs():
     runs["cases"].extend(logcut_cases(r))
     runs["cases"].extend(wfcut_cases(r))
     runs["cases"].extend(dcs_cases(r))
+    runs["cases"].extend(section_cases(r))
     # random functions (run_random_function_omp): cross section and DOS, seeds 1..nseed, sorted bins
     for kind, d, n in (("crsec", 3, 60), ("dos", 3, 60), ("dos", 2, 80)):
         data = r.random_function(kind, d, n, 5, 4, 0.4, 3.5)
@@ -278,6 +279,51 @@ def dcs_cases(r):
     return out
 
 
+def section_cases(r):
+    """The [medium], [kcut], [kplane], [random_function] and [eigenstate_list]
+    sections the reference's own writers append for seeded values, including
+    signed zeros and NaNs, infinities and extreme exponents."""
+    rng = np.random.default_rng(21)
+    odd = [complex(-0.0, 0.0), complex(np.copysign(np.nan, -1.0), np.nan), complex(np.inf, -np.inf),
+           complex(1e-300, -2.5e300), complex(np.nan, np.copysign(np.nan, -1.0))]
+
+    def cvals(m):
+        v = list(rng.standard_normal(m) * 10.0 ** rng.integers(-8, 9, m) + 1j * rng.standard_normal(m))
+        return v[:max(0, m - len(odd))] + odd[:m]
+
+    def cl(z):
+        """IEEE bit patterns (JSON keeps neither a NaN's sign nor -0 reliably): re, im, ..."""
+        return np.ascontiguousarray(np.asarray(z, dtype=np.complex128)).view(np.uint64).tolist()
+
+    out = {"kind": "dat_sections"}
+    out["medium"] = [{"d": d, "n": n, "model": mo, "params": list(pa), "shape": sh, "ratio": ra,
+                      "text": r.save_medium(d, n, mo, pa, sh, ra)}
+                     for d, n, mo, pa, sh, ra in ((3, 1024, "maximum", (), "ball", 1.0),
+                                                   (2, 50, "resonant", (1.5, 0.25), "cube", 2.5))]
+    kc = cvals(15)
+    out["kcut"] = {"ns": 3, "zmin": [0.5, -0.05], "zmax": [3.0, -0.05], "nseed": 2, "title": "Trace-log",
+                   "realtime": 1.25, "data": cl(kc),
+                   "text": r.save_kcut(3, complex(0.5, -0.05), complex(3.0, -0.05), 2, "Trace-log", 1.25, kc)}
+    kp = cvals(6)
+    out["kplane"] = {"nx": 3, "ny": 2, "xrange": [0.5, 3.0], "yrange": [-0.5, 0.0], "nseed": 3, "title": "Map",
+                     "realtime": 12.5, "color": "viridis div 2.5 rev", "data": cl(kp),
+                     "text": r.save_kplane(3, 2, 0.5, 3.0, -0.5, 0.0, 3, "Map", 12.5, "viridis div 2.5 rev", kp)}
+    rf = rng.standard_normal(6) * 1e3
+    rf[1] = np.copysign(np.nan, -1.0)
+    rf[4] = -0.0
+    out["random_function"] = {"kind": "dos", "nseed": 2, "nbin": 3, "xmin": 0.4, "xmax": 3.5, "title": "DOS",
+                              "realtime": 2.0, "data": rf.view(np.uint64).tolist(),
+                              "text": r.save_rfun("dos", 2, 3, 0.4, 3.5, "DOS", 2.0, rf)}
+    kr, mu = cvals(2), [complex(1e-12, 2e-13), complex(0.0, -3e-11)]
+    ev = [cvals(4), cvals(4)]
+    out["eigenstate_list"] = {"d": 3, "n": 4, "seed": 7, "method": "mineigval", "ntarget": 32,
+                              "dom": [0.5, 3.0, -1.0, 0.0], "maxit": 30, "toler": 1e-10, "verb": 0,
+                              "realtime": 0.75, "kroot": cl(kr), "mu": cl(mu), "eigv": [cl(v) for v in ev],
+                              "text": r.save_eigls(3, 4, 7, "mineigval", 32, [0.5, 3.0, -1.0, 0.0], 30, 1e-10, 0,
+                                                   0.75, kr, mu, ev)}
+    return [out]
+
+
 if __name__ == "__main__":
     if "--chistogram-only" in sys.argv:
         # add or refresh only the mu-plane histogram cases of an existing reference_runs.json
@@ -288,8 +334,9 @@ if __name__ == "__main__":
         r = Reference()
         runs["cases"] = [c for c in runs["cases"] if c["kind"] not in ("chistogram", "imag_mu", "wavefunction_file",
                                                                        "logcut", "wfcut_stats",
-                                                                       "wavefunction_cut_file", "diff_cross_section")
-                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r) + wfcut_cases(r) + dcs_cases(r)
+                                                                       "wavefunction_cut_file", "diff_cross_section",
+                                                                       "dat_sections")
+                         and c.get("mtype") != "normalized"] + chistogram_cases(r) + logcut_cases(r) + wfcut_cases(r) + dcs_cases(r) + section_cases(r)
         with open(path, "w") as f:
             json.dump(runs, f, indent=0)
         sys.exit(0)

@@ -83,3 +83,43 @@ def test_logcut_mesh_and_section_match_reference(ref_runs, tmp_path):
     assert f.read_text() == c["text"]
     with pytest.raises(ValueError):
         ms.logcut_args(10, 2.5, 1e-6, -0.4)
+
+
+def test_sections_match_reference_writers(ref_runs, tmp_path):
+    """[medium], [kcut], [kplane], [random_function] and [eigenstate_list] byte for
+    byte as the reference's own writers append them (tests/golden, kind
+    dat_sections), signed zeros, signed NaNs, infinities and extreme exponents
+    included."""
+    c = [c for c in ref_runs["cases"] if c["kind"] == "dat_sections"][0]
+
+    def bits_c(b):  # the fixture keeps the values' IEEE bit patterns
+        return np.array(b, dtype=np.uint64).view(np.complex128)
+
+    def written(fn):
+        f = tmp_path / "s.dat"
+        if f.exists():
+            f.unlink()
+        fn(str(f))
+        return f.read_text()
+
+    for m in c["medium"]:
+        assert written(lambda f: datio.save_medium(f, m["d"], m["n"], m["model"], m["params"], m["shape"],
+                                                   m["ratio"])) == m["text"]
+    k = c["kcut"]
+    assert written(lambda f: datio.save_complexcut(f, bits_c(k["data"]), k["ns"], complex(*k["zmin"]),
+                                                   complex(*k["zmax"]), k["title"], k["realtime"],
+                                                   k["nseed"])) == k["text"]
+    p = c["kplane"]
+    col = p["color"].split()
+    assert written(lambda f: datio.save_complexmap(f, bits_c(p["data"]), p["nx"], p["ny"], p["xrange"], p["yrange"],
+                                                   p["title"], p["realtime"], p["nseed"],
+                                                   (col[0], col[1], float(col[2]), len(col) > 3))) == p["text"]
+    r = c["random_function"]
+    data = np.array(r["data"], dtype=np.uint64).view(np.float64).reshape(r["nbin"], r["nseed"])
+    assert written(lambda f: datio.save_random_function(f, r["kind"], data, r["xmin"], r["xmax"], r["title"],
+                                                        r["realtime"])) == r["text"]
+    e = c["eigenstate_list"]
+    states = list(zip(bits_c(e["kroot"]), bits_c(e["mu"]), [bits_c(v) for v in e["eigv"]]))
+    assert written(lambda f: datio.save_eigenstate_list(f, states, e["seed"], e["method"], e["ntarget"], e["dom"],
+                                                        e["maxit"], e["toler"], e["realtime"],
+                                                        e["verb"])) == e["text"]
