@@ -80,3 +80,12 @@ def test_total_cross_section_goldens(oracle, ref_tests):
     for k, want in zip(g["ks"], g["expected"]):
         got = oracle.total_cross_section(m["d"], g["n"], pos, k, m["model"], m["params"])
         assert rel(got, want) < 1e-10
+
+
+def test_psi_grid_is_the_wavefunction_grid(oracle):
+    """The grid part alone (timed by the C5 CPU baseline) gives the combined
+    solve-and-grid routine's psi bit for bit, from its amplitudes."""
+    pos = oracle.fill_medium(3, 60, 1)
+    dom = [-6.0, 6.0, -5.0, 5.0]
+    amp, psi = oracle.wavefunction(3, 60, pos, 1.5 - 0.01j, 12, 10, dom)
+    assert np.array_equal(oracle.psi_grid(3, 60, pos, 1.5 - 0.01j, 12, 10, dom, amp), psi)
