@@ -176,3 +176,26 @@ def test_host_entries_say_why_they_reject_arguments(libpath):
     assert L.msgpu_random_function(4, 3, 10, 1, 1.0, C.byref(m), 2, 4, 0.5, 2.5, data, np.zeros(8, dtype=np.int32),
                                    0) == -1
     assert b"random_function" in L.msgpu_last_error()
+
+
+def test_task_dropins_refuse_without_the_reference_helpers(libpath, tmp_path):
+    """In a program without the reference's fill_chist, append_list_ihist,
+    normalize_ihist, alloc/check_eigenstate_list and store_data_wfcut, the task
+    drop-ins that hand their results to those functions print an error and
+    return before any device work, as does a wavefunction with a spherical
+    source; no GPU is touched, so this runs anywhere."""
+    exe = tmp_path / "refusals"
+    src = os.path.join(ROOT, "tests", "dropin_refusals_check.c")
+    r = subprocess.run(["gcc", "-O1", "-std=gnu11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src,
+                        "-o", str(exe), libpath, "-Wl,-rpath," + os.path.dirname(libpath), "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    lines = out.stdout.splitlines()
+    for name in ("run_chistogram_omp", "run_imag_mu_histogram_omp", "compute_eigenstates",
+                 "run_wave_function_cut_omp"):
+        assert any(l.startswith(f"[ERROR] {name}:") and "not linked in" in l for l in lines), (name, lines)
+    assert any(l.startswith("[ERROR] run_wave_function_omp:") and "plane" in l for l in lines), lines
+    assert "done chist" in lines and "done ihist 0" in lines and "done eigls 0" in lines
+    assert "done wfcut 0" in lines and "done wfun 0" in lines
