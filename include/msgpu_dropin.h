@@ -5,7 +5,12 @@
  * users, the tests) relink against the GPU without source changes.
  *
  * The structs below are layout-identical to the reference types they stand
- * for; only the fields the hot path reads are named meaningfully.
+ * for, field for field and under the reference's field names
+ * (tests/test_dropin_layouts.py asserts every size and offset against the
+ * reference's own headers).  The task drop-ins hand their results to the
+ * reference's own histogram, eigenstate-list and cut-statistics functions
+ * through weak references, resolved from the program they are linked into;
+ * without those functions they print an error and return.
  */
 #ifndef MSGPU_DROPIN_H
 #define MSGPU_DROPIN_H
