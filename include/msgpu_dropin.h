@@ -1,8 +1,9 @@
 /*
  * msgpu_dropin.h -- symbol-compatible replacements for the reference's own
- * hot-path functions.  libmsgpu.so exports these names with the reference's
- * signatures, so the reference's callers (src/core/ms_core.c, root_finder.c
- * users, the tests) relink against the GPU without source changes.
+ * hot-path functions and for every task driver of src/core/ms_core.c.
+ * libmsgpu.so exports these names with the reference's signatures, so the
+ * reference's callers (src/core/ms_core.c, root_finder.c users, the tests)
+ * relink against the GPU without source changes.
  *
  * The structs below are layout-identical to the reference types they stand
  * for, field for field and under the reference's field names
